@@ -1,0 +1,332 @@
+"""Benchmark: Mrays/s of the GB300 path tracer on the 256-icosphere scene.
+
+Workload (one step = one frame): 256 level-4 icospheres (1.31 M triangles, one
+BLAS each + TLAS), 1 directional + 4 point + 2 spot lights, constant background
+0.1, 1920x1080, 8 samples per pixel, path depth 8, Russian roulette from bounce
+4 (kuafu's defaults). Rays = primary + extension + shadow traversals actually
+issued; BVH build is outside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank renders its own replica of the workload (the
+path has no cross-GPU exchange); value = rays of all ranks / max time over ranks.
+--impl reference times the CPU implementation (the oracle port of kuafu's
+shaders) on the host cores over a bounded crop of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(width=1920, height=1080, spp=8, depth=8, count=256, level=4, seed=0)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"kf_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(device: int, profile=False, debug=False):
+    from kuafu_gb300 import api, scenes
+
+    cfg = scenes.icosphere_config(spp=WORKLOAD["spp"], depth=WORKLOAD["depth"], seed=WORKLOAD["seed"],
+                                  count=WORKLOAD["count"])
+    cfg._c.device = device
+    cfg.setProfile(profile)
+    cfg.setDebugOutputs(debug)
+    r = api.Kuafu(cfg)
+    cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
+                            level=WORKLOAD["level"], seed=WORKLOAD["seed"])
+    return r, cam
+
+
+def cpu_baseline_sample(seconds_target=12.0, threads=0):
+    """The oracle on the host cores over a centred crop, sized for ~10-30 s of work."""
+    from kuafu_gb300 import api, scenes
+    from oracle import oracle as O
+
+    cfg = scenes.icosphere_config(spp=WORKLOAD["spp"], depth=WORKLOAD["depth"], count=WORKLOAD["count"])
+    cfg.setHostOnly(True)
+    r = api.Kuafu(cfg)
+    cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
+                            level=WORKLOAD["level"], seed=WORKLOAD["seed"])
+    flat = r.getScene().export()
+    ubo = cam.ubo()
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    pc = O.push_constants(WORKLOAD["spp"], WORKLOAD["depth"], clear=(0.1, 0.1, 0.1, 1.0), rr=True, rr_min=4)
+    nthreads = threads or os.cpu_count() or 1
+    side = 32
+    while True:
+        x0, y0 = (W - side) // 2, (H - side) // 2
+        t0 = time.perf_counter()
+        res = O.render(flat, ubo, W, H, pc, seed=WORKLOAD["seed"], frame=0, camera_index=1, use_bvh=True,
+                       threads=nthreads, crop=(x0, y0, side, side), want_paths=False, want_hits=False)
+        dt = time.perf_counter() - t0
+        rays = sum(res["rays"])
+        if dt >= seconds_target / 4 or side >= 512:
+            break
+        side = min(512, int(side * max(1.5, (seconds_target / 4 / max(dt, 1e-3)) ** 0.5)))
+    r.close()
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": f"{side}x{side} centre crop of the 1920x1080 frame, {WORKLOAD['spp']} spp, depth "
+                      f"{WORKLOAD['depth']}, {rays} rays in {dt:.2f} s"}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    samples = []
+    base = None
+    for step in range(args.warmup + args.steps):
+        b = cpu_baseline_sample(seconds_target=8.0 if step < args.warmup else 10.0)
+        if step >= args.warmup:
+            samples.append(b["value"])
+            base = b
+    v = statistics.median(samples)
+    line = {"impl": "reference", "metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "icospheres-256 1920x1080 8spp depth8", **WORKLOAD},
+            "cpu_baseline": {**base, "value": v},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    from kuafu_gb300 import _native as N
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    device = local
+    r, cam = build_scene(device)
+    stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", device))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+
+    # warm-up (also builds BLAS / TLAS and captures the frame graph)
+    for _ in range(max(args.warmup, 1)):
+        r.run()
+    r.synchronize()
+    r.resetStats()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    clocks = ClockSampler(device)
+    times = []
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)  # L2 flush between steps, outside the timed events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        r.run()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    st = r.stats()
+    rays = st.rays_primary + st.rays_extension + st.rays_shadow
+    t_ms = sum(times)
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([t_ms], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+        rr = torch.tensor([float(rays)], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(rr)
+        rays_all = float(rr.item())
+    else:
+        rays_all = float(rays)
+    value = rays_all / (t_ms / 1e3) / 1e6
+    rays_per_frame = rays / args.steps
+
+    # e2e: the public API with host buffers: run + download of the BGRA frame per step
+    host = torch.empty((WORKLOAD["height"], WORKLOAD["width"], 4), dtype=torch.uint8).pin_memory()
+    r.resetStats()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.run()
+        N.check(N.load().kf_renderer_download_latest_frame(r._h, cam._h, host.data_ptr(), host.numel()))
+    e2e_s = time.perf_counter() - t0
+    st2 = r.stats()
+    e2e_rays = st2.rays_primary + st2.rays_extension + st2.rays_shadow
+    e2e_val = e2e_rays / e2e_s / 1e6 * ws
+    h2d = C.sizeof(N.kf_camera_ubo) + C.sizeof(N.kf_push_constants) + 32 + C.sizeof(N.kf_dir_light_ubo) + \
+        C.sizeof(N.kf_point_lights_ubo) + C.sizeof(N.kf_active_lights_ubo)
+
+    result = None
+    if rank == 0:
+        # per-kernel durations (CUDA events around each launch) and algorithmic bytes (counting pass)
+        r.close()
+        rp, _ = build_scene(device, profile=True)
+        rp.run()
+        rp.resetStats()
+        rp.run()
+        sp = rp.stats()
+        rp.countTraversal(True)
+        rp.resetStats()
+        rp.run()
+        sc = rp.stats()
+        rp.close()
+        launches = WORKLOAD["depth"] + 1
+        node_b, tri_b, inst_b = 128, 48, 64
+        ext_bytes = sc.node_visits * node_b + sc.tri_tests * tri_b + sc.inst_visits * inst_b
+        sh_bytes = sc.shadow_node_visits * node_b + sc.shadow_tri_tests * tri_b + sc.shadow_inst_visits * inst_b
+        peak, peak_kind = _peaks()
+        dom_ext = sp.extend_ms >= sp.shadow_ms
+        k_bytes, k_ms = (ext_bytes, sp.extend_ms) if dom_ext else (sh_bytes, sp.shadow_ms)
+        achieved = k_bytes / launches / (k_ms / launches / 1e3) / 1e9 if k_ms > 0 else None
+        traffic = None
+        tf = ROOT / "profiles" / "traffic.json"
+        if tf.exists():
+            try:
+                traffic = json.loads(tf.read_text()).get("extend_dram_bytes_per_launch" if dom_ext else
+                                                         "shadow_dram_bytes_per_launch")
+            except Exception:
+                traffic = None
+        cpu = cpu_baseline_sample()
+        result = {
+            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "icospheres-256 1920x1080 8spp depth8", **WORKLOAD,
+                       "triangles": WORKLOAD["count"] * 20 * 4 ** WORKLOAD["level"],
+                       "rays_per_frame": rays_per_frame, "l2": "flushed (512 MiB write) before every timed step",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "kernel": "k_extend" if dom_ext else "k_shadow",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "bytes_per_ray": (k_bytes / ((sc.rays_primary + sc.rays_extension) if dom_ext else
+                                                      max(sc.rays_shadow, 1))),
+                         "kernel_ms_per_frame": {"extend": sp.extend_ms, "shade": sp.shade_ms,
+                                                 "shadow": sp.shadow_ms, "frame": sp.frame_ms}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": WORKLOAD["width"] * WORKLOAD["height"] * 4},
+            "clocks": clk,
+            "gpu_launches": args.steps * (1 + 4 * (WORKLOAD["depth"] + 1) + 2),
+        }
+        print(json.dumps(result), flush=True)
+    else:
+        r.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from kuafu_gb300 import build
+
+    build.build_oracle()
+    build.build_libkf()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,259 @@
+/*
+ * kf.h — C-ABI of libkf, the GB300-native replacement for kuafu's render path.
+ *
+ * kuafu exposes a C++ class API (include/kuafu.hpp, include/core/{scene,camera,
+ * geometry,light,config}.hpp); SAPIEN links it as libkuafu.so. This header is
+ * the flat, exception-free boundary underneath an equivalent C++ facade
+ * (include/kuafu_gb300/kuafu.hpp): plain pointers and sizes, opaque handles,
+ * int status codes and a thread-local error string. Every entry point names the
+ * kuafu function it replaces.
+ *
+ * Threading: like kuafu (single-threaded, mutable globals) a renderer and the
+ * objects created from it must be used from one thread at a time.
+ */
+#ifndef KF_H
+#define KF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "kf_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define KF_API __declspec(dllexport)
+#else
+#define KF_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes (kuafu throws std::runtime_error: stdafx.hpp:61-67) ---- */
+#define KF_OK 0
+#define KF_ERR_INVALID_ARGUMENT 1 /* KF_ASSERT failures on bad handles / values */
+#define KF_ERR_OUT_OF_RANGE 2     /* scene.cpp:54 "Geometry Instances out of bound." */
+#define KF_ERR_LIMIT 3            /* scene.cpp:61,116 buffer size exceeded */
+#define KF_ERR_CUDA 4             /* device / driver failure */
+#define KF_ERR_NOT_IMPLEMENTED 5  /* scene.cpp:153,157 "Not implemented!" */
+#define KF_ERR_STATE 6            /* call order violated (e.g. render without camera) */
+#define KF_ERR_NO_DEVICE 7        /* no CUDA device: there is no CPU fallback */
+#define KF_ERR_OUT_OF_MEMORY 8
+#define KF_ERR_INTERNAL 9
+#define KF_ERR_TIMEOUT 10         /* a bounded device-side wait gave up */
+
+/* Thread-local message of the last failing call on this thread. */
+KF_API const char* kf_last_error(void);
+KF_API int kf_version(void);
+
+typedef struct kf_renderer_s* kf_renderer; /* kuafu::Kuafu */
+typedef struct kf_scene_s* kf_scene;       /* kuafu::Scene */
+typedef struct kf_camera_s* kf_camera;     /* kuafu::Camera */
+typedef struct kf_geometry_s* kf_geometry; /* std::shared_ptr<kuafu::Geometry> */
+typedef struct kf_instance_s* kf_instance; /* std::shared_ptr<kuafu::GeometryInstance> */
+typedef struct kf_light_s* kf_light;       /* std::shared_ptr<PointLight / ActiveLight> */
+
+/* ---- kuafu::Config (include/core/config.hpp:35-177) ---- */
+typedef struct kf_config {
+    int32_t initial_width;         /* setInitialWidth  (default 800) */
+    int32_t initial_height;        /* setInitialHeight (default 600) */
+    uint32_t spp;                  /* setPerPixelSampleRate (default 32) */
+    uint32_t path_depth;           /* setPathDepth (default 8) */
+    uint32_t max_path_depth;       /* getMaxPathDepth (12) */
+    uint32_t russian_roulette;     /* setRussianRoulette (default 1) */
+    uint32_t rr_min_bounces;       /* setRussianRouletteMinBounces (default 4) */
+    uint32_t nee;                  /* setNextEventEstimation (default 1, unused as in kuafu) */
+    uint32_t nee_min_bounces;      /* setNextEventEstimationMinBounces (default 0, unused) */
+    uint32_t accumulate_frames;    /* setAccumulatingFrames (default 1) */
+    uint32_t use_denoiser;         /* setUseDenoiser (default 0) */
+    uint32_t present;              /* setPresent: accepted, rendering is always headless */
+    uint32_t max_geometries;       /* setGeometryLimit (default 128) */
+    uint32_t max_instances;        /* setGeometryInstanceLimit (default 256) */
+    uint32_t max_textures;         /* setTextureLimit (default 128) */
+    uint32_t max_materials;        /* setMaterialLimit (default 256) */
+    /* GB300 additions */
+    uint32_t seed;                 /* Philox seed (key word 0 is seed ^ pixel_index) */
+    uint32_t blas_leaf_size;       /* max triangles per BVH leaf (default 4) */
+    uint32_t tlas_leaf_size;       /* max instances per TLAS leaf (default 1) */
+    uint64_t max_paths_in_flight;  /* wavefront chunk size (default 1<<24) */
+    uint32_t debug_outputs;        /* 1: keep per-path radiance and primary hits for download */
+    uint32_t profile;              /* 1: time kernels with CUDA events (kf_stats.*_ms) */
+    uint32_t use_graph;            /* 1: replay the per-frame launch sequence as a CUDA graph (default 1) */
+    uint32_t device;               /* CUDA device ordinal (default 0) */
+    uint32_t host_only;            /* 1: scene management and export only, no device is touched;
+                                      rendering calls then fail with KF_ERR_NO_DEVICE */
+} kf_config;
+
+/* Fills kuafu's defaults (config.hpp:140-176). */
+KF_API void kf_config_init(kf_config* cfg);
+
+/* ---- kuafu::Kuafu (include/kuafu.hpp:31-93, src/kuafu.cpp) ---- */
+KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out);          /* Kuafu(config), kuafu.cpp:27-63 */
+KF_API int kf_renderer_destroy(kf_renderer r);
+KF_API int kf_renderer_get_config(kf_renderer r, kf_config* out);               /* Kuafu::getConfig */
+KF_API int kf_renderer_set_config(kf_renderer r, const kf_config* cfg);         /* Config setters */
+KF_API int kf_renderer_get_scene(kf_renderer r, kf_scene* out);                 /* Kuafu::getScene */
+KF_API int kf_renderer_create_scene(kf_renderer r, kf_scene* out);              /* Kuafu::createScene */
+KF_API int kf_renderer_set_scene(kf_renderer r, kf_scene s);                    /* Kuafu::setScene */
+KF_API int kf_renderer_remove_scene(kf_renderer r, kf_scene s);                 /* Kuafu::removeScene */
+KF_API int kf_renderer_is_running(kf_renderer r, int* out);                     /* Kuafu::isRunning */
+/* Renders one frame of the current scene through its current camera: spp samples
+ * per pixel, accumulated into the camera's running mean (Kuafu::run, kuafu.cpp:72-85;
+ * Context::render, context.cpp:522-540). Work is queued on the renderer's stream. */
+KF_API int kf_renderer_run(kf_renderer r);
+KF_API int kf_renderer_synchronize(kf_renderer r);
+/* The cudaStream_t every kernel of this renderer is launched on (for CUDA-event timing). */
+KF_API int kf_renderer_get_stream(kf_renderer r, void** out_stream);
+/* Latest frame as sRGB-encoded BGRA8, w*h*4 bytes (Kuafu::downloadLatestFrame,
+ * kuafu.cpp:87-95; Camera::downloadLatestFrame, camera.cpp:188-207). */
+KF_API int kf_renderer_download_latest_frame(kf_renderer r, kf_camera cam, uint8_t* out_bgra, size_t bytes);
+
+/* Extra render targets of a camera (rt.cpp:497-512 + depth). */
+enum {
+    KF_AOV_RADIANCE_F32 = 0,  /* float4 per pixel: the accumulated "rgba" target */
+    KF_AOV_ALBEDO_F32 = 1,    /* float4 per pixel: "albedo" target */
+    KF_AOV_NORMAL_F32 = 2,    /* float4 per pixel: "normal" target */
+    KF_AOV_DEPTH_F32 = 3,     /* float per pixel: primary-hit distance (0 on miss), sample 0 */
+    KF_AOV_SUM_F64 = 4,       /* double4 per pixel: FP64 sum of every frame's finalColor */
+    KF_AOV_PATH_RADIANCE = 5, /* float4 per path [spp][h][w] of the last frame (debug_outputs) */
+    KF_AOV_PRIMARY_HITS = 6,  /* kf_hit per path [spp][h][w] of the last frame (debug_outputs) */
+    KF_AOV_DENOISED_F32 = 7   /* float4 per pixel: output of the learned denoiser */
+};
+KF_API int kf_renderer_download_aov(kf_renderer r, kf_camera cam, int kind, void* out, size_t bytes);
+
+typedef struct kf_stats {
+    uint64_t frames;
+    uint64_t rays_primary;
+    uint64_t rays_extension;
+    uint64_t rays_shadow;
+    uint64_t node_visits;     /* closest-hit traversal; counted only with kf_renderer_count_traversal */
+    uint64_t tri_tests;
+    uint64_t inst_visits;
+    uint64_t shadow_node_visits; /* any-hit (shadow) traversal; counted only with kf_renderer_count_traversal */
+    uint64_t shadow_tri_tests;
+    uint64_t shadow_inst_visits;
+    double extend_ms;         /* summed CUDA-event durations (profile = 1) */
+    double shadow_ms;
+    double shade_ms;
+    double frame_ms;
+    double bvh_build_ms;
+    int32_t frame_count;      /* kuafu's global::frameCount */
+    uint32_t last_spp;
+    uint32_t blas_nodes;
+    uint32_t tlas_nodes;
+} kf_stats;
+KF_API int kf_renderer_get_stats(kf_renderer r, kf_stats* out);
+KF_API int kf_renderer_reset_stats(kf_renderer r);
+/* Re-trace the last frame's traversal with per-ray counters (node / triangle /
+ * instance visits) to give algorithmic bytes per ray. */
+KF_API int kf_renderer_count_traversal(kf_renderer r, int enable);
+
+/* ---- process-global material table (global.hpp:33-35, geometry.cpp:241-249) ---- */
+typedef struct kf_material {       /* kuafu::NiceMaterial (geometry.hpp:11-30) */
+    float diffuse_color[3];
+    float alpha;
+    float metallic;
+    float specular;
+    float roughness;
+    float ior;
+    float transmission;
+    float emission[3];
+    float emission_strength;
+    int32_t diffuse_tex;            /* texture ids from kf_texture_create, -1 = none */
+    int32_t metallic_tex;
+    int32_t roughness_tex;
+    int32_t transmission_tex;
+} kf_material;
+KF_API void kf_material_init(kf_material* m);             /* NiceMaterial defaults */
+KF_API int kf_material_add(const kf_material* m, uint32_t* out_index);
+KF_API uint32_t kf_material_count(void);
+KF_API int kf_material_get(uint32_t index, kf_material* out);
+KF_API int kf_material_clear(void);
+
+/* ---- textures (vkCore::Texture: RGBA8, sRGB, linear/repeat sampler) ---- */
+KF_API int kf_texture_create(const uint8_t* rgba8, uint32_t width, uint32_t height, int srgb, int32_t* out_id);
+KF_API uint32_t kf_texture_count(void);
+
+/* ---- kuafu::Geometry (geometry.hpp:32-46) ---- */
+KF_API int kf_geometry_create(const kf_vertex* vertices, uint32_t num_vertices, const uint32_t* indices,
+                              uint32_t num_indices, const uint32_t* mat_index, uint32_t num_mat_index,
+                              kf_geometry* out);
+KF_API int kf_geometry_set_material(kf_geometry g, const kf_material* m);   /* Geometry::setMaterial */
+KF_API int kf_geometry_set_flags(kf_geometry g, int opaque, int hide_render, int dynamic_);
+KF_API int kf_geometry_recalculate_normals(kf_geometry g);                  /* Geometry::recalculateNormals */
+KF_API int kf_geometry_get_info(kf_geometry g, uint32_t* num_vertices, uint32_t* num_indices);
+KF_API int kf_geometry_get_data(kf_geometry g, kf_vertex* vertices, uint32_t* indices, uint32_t* mat_index);
+KF_API int kf_geometry_release(kf_geometry g);
+/* Procedural meshes (geometry.cpp:297-537) plus the level-n icosphere. */
+enum { KF_MESH_YZ_PLANE = 0, KF_MESH_CUBE = 1, KF_MESH_SPHERE = 2, KF_MESH_CAPSULE = 3, KF_MESH_ICOSPHERE = 4 };
+KF_API int kf_geometry_create_builtin(int kind, float param0, float param1, const kf_material* m, kf_geometry* out);
+
+/* ---- kuafu::Scene (include/core/scene.hpp:40-295, src/core/scene.cpp) ---- */
+KF_API int kf_scene_submit_geometry(kf_scene s, kf_geometry g);             /* submitGeometry */
+KF_API int kf_scene_clear_geometries(kf_scene s);                          /* clearGeometries */
+KF_API int kf_scene_remove_geometry(kf_scene s, kf_geometry g);            /* removeGeometry: not implemented in kuafu */
+KF_API int kf_scene_submit_instance(kf_scene s, kf_geometry g, const float transform[16], kf_instance* out);
+KF_API int kf_instance_set_transform(kf_instance i, const float transform[16]);  /* GeometryInstance::setTransform */
+KF_API int kf_scene_remove_instance(kf_scene s, kf_instance i);            /* removeGeometryInstance */
+KF_API int kf_scene_clear_instances(kf_scene s);                           /* clearGeometryInstances */
+KF_API int kf_scene_instance_count(kf_scene s, uint32_t* out);
+KF_API int kf_scene_get_instance(kf_scene s, uint32_t index, kf_instance* out);  /* getGeometryInstance */
+KF_API int kf_instance_release(kf_instance i);
+KF_API int kf_scene_set_clear_color(kf_scene s, const float rgba[4]);      /* setClearColor */
+KF_API int kf_scene_get_clear_color(kf_scene s, float rgba[4]);
+KF_API int kf_scene_mark_geometries_changed(kf_scene s);
+KF_API int kf_scene_mark_instances_changed(kf_scene s);
+
+typedef struct kf_directional_light { float direction[3]; float color[3]; float strength; float softness; } kf_directional_light; /* light.hpp:9-14 */
+typedef struct kf_point_light { float position[3]; float color[3]; float radius; float strength; } kf_point_light;             /* light.hpp:16-21 */
+typedef struct kf_active_light { float view[16]; float color[3]; float fov; float strength; float softness; int32_t tex_id; } kf_active_light; /* light.hpp:31-39 */
+
+KF_API int kf_scene_set_directional_light(kf_scene s, const kf_directional_light* l);  /* setDirectionalLight */
+KF_API int kf_scene_remove_directional_light(kf_scene s);                              /* removeDirectionalLight */
+KF_API int kf_scene_add_point_light(kf_scene s, const kf_point_light* l, kf_light* out);   /* addPointLight */
+KF_API int kf_scene_add_active_light(kf_scene s, const kf_active_light* l, kf_light* out); /* addActiveLight */
+KF_API int kf_light_update_point(kf_light l, const kf_point_light* p);
+KF_API int kf_light_update_active(kf_light l, const kf_active_light* a);
+KF_API int kf_scene_remove_light(kf_scene s, kf_light l);                  /* removePointLight / removeActiveLight */
+
+KF_API int kf_scene_create_camera(kf_scene s, int width, int height, kf_camera* out);  /* createCamera */
+KF_API int kf_scene_remove_camera(kf_scene s, kf_camera c);                /* removeCamera */
+KF_API int kf_scene_set_camera(kf_scene s, kf_camera c);                   /* setCamera */
+KF_API int kf_scene_get_camera(kf_scene s, kf_camera* out);                /* getCamera */
+
+/* Flattened scene as the kernels consume it (scene.cpp:231-467). Pointers stay
+ * valid until the scene changes. Used by tests to feed the oracle. */
+KF_API int kf_scene_export(kf_scene s, kf_flat_scene* out);
+
+/* ---- kuafu::Camera (include/core/camera.hpp:40-174, src/core/camera.cpp) ---- */
+KF_API int kf_camera_set_position(kf_camera c, const float p[3]);          /* setPosition */
+KF_API int kf_camera_set_front(kf_camera c, const float f[3]);             /* setFront */
+KF_API int kf_camera_set_up(kf_camera c, const float u[3]);                /* setUp */
+KF_API int kf_camera_set_pose(kf_camera c, const float pose[16]);          /* setPose */
+KF_API int kf_camera_get_pose(kf_camera c, float pose[16]);                /* getPose */
+KF_API int kf_camera_set_full_perspective(kf_camera c, float width, float height, float fx, float fy, float cx,
+                                          float cy, float skew);          /* setFullPerspective */
+KF_API int kf_camera_set_size(kf_camera c, int width, int height);         /* setSize */
+KF_API int kf_camera_reset_view(kf_camera c);                              /* resetView */
+KF_API int kf_camera_get_size(kf_camera c, int* width, int* height);
+KF_API int kf_camera_get_ubo(kf_camera c, kf_camera_ubo* out);             /* uploadCameraBuffer, scene.cpp:236-250 */
+
+/* ---- batched offscreen rendering: many cameras / scenes in one launch sequence ---- */
+typedef struct kf_batch_item {
+    kf_scene scene;
+    kf_camera camera;
+    uint32_t spp;
+    uint32_t pad;
+} kf_batch_item;
+KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint32_t count);
+
+/* ---- FP64 relative-MSE reduction: mean over pixels and channels of
+ * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64 ---- */
+KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
+                     double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KF_H */

@@ -1,0 +1,1009 @@
+// kf_api.cu — the C-ABI (include/kf.h): exception-free entry points over the
+// host object model. Each function mirrors the kuafu method named in kf.h.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "kf_host.h"
+
+namespace kf {
+std::mutex& global_mutex() {
+    static std::mutex m;
+    return m;
+}
+std::vector<kf_material> g_materials;
+std::vector<HostTexture> g_textures;
+uint64_t g_material_version = 1, g_texture_version = 1;
+
+// sRGB transfer tables computed in FP64 (IEC 61966-2-1 piecewise curve).
+const std::vector<float>& srgb_decode_table() {
+    static const std::vector<float> t = [] {
+        std::vector<float> v(256);
+        for (int i = 0; i < 256; ++i) {
+            const double c = i / 255.0;
+            v[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        return v;
+    }();
+    return t;
+}
+// thresh[k] = linear value at which the 8-bit sRGB code reaches k (k - 0.5 on the code axis).
+const std::vector<float>& srgb_threshold_table() {
+    static const std::vector<float> t = [] {
+        std::vector<float> v(256);
+        v[0] = -INFINITY;
+        for (int k = 1; k < 256; ++k) {
+            const double c = (k - 0.5) / 255.0;
+            v[k] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        return v;
+    }();
+    return t;
+}
+} // namespace kf
+
+using namespace kf;
+
+namespace {
+thread_local std::string t_error;
+
+int fail(int code, const std::string& msg) {
+    t_error = msg;
+    return code;
+}
+
+template <class F> int guarded(F&& f) {
+    try {
+        f();
+        return KF_OK;
+    } catch (const KfError& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(KF_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(KF_ERR_INTERNAL, e.what());
+    }
+}
+
+#define REQ(cond, msg) KF_REQUIRE(cond, KF_ERR_INVALID_ARGUMENT, msg)
+
+void camera_init(kf_camera_s* c, int w, int h) {
+    // Camera::Camera (camera.cpp:8-18) + resetView (camera.cpp:20-30)
+    c->width = w;
+    c->height = h;
+    c->cx = (float)w * 0.5f;
+    c->cy = (float)h * 0.5f;
+    c->fx = c->fy = (float)w * 0.5f;
+    camera_update_proj(c);
+    c->position[0] = c->position[1] = c->position[2] = 0.0f;
+    const float up[3] = {0, 0, 1}, right[3] = {0, -1, 0}, front[3] = {1, 0, 0};
+    std::memcpy(c->up, up, sizeof(up));
+    std::memcpy(c->right, right, sizeof(right));
+    std::memcpy(c->front, front, sizeof(front));
+    camera_update_view(c);
+}
+
+kf_camera_s* scene_new_camera(kf_scene_s* s, int w, int h) {
+    auto cam = std::make_unique<kf_camera_s>();
+    cam->scene = s;
+    camera_init(cam.get(), w, h);
+    s->cameras.push_back(std::move(cam));
+    return s->cameras.back().get();
+}
+
+kf_scene_s* new_scene(kf_renderer_s* r) {
+    auto s = std::make_unique<kf_scene_s>();
+    s->renderer = r;
+    s->current_camera = scene_new_camera(s.get(), 1, 1); // Scene::Scene (scene.hpp:215-217)
+    r->scenes.push_back(std::move(s));
+    return r->scenes.back().get();
+}
+
+void geometry_retain(kf_geometry_s* g) { g->refs.fetch_add(1); }
+void geometry_release(kf_geometry_s* g) {
+    if (g && g->refs.fetch_sub(1) == 1) delete g;
+}
+void instance_release(kf_instance_s* i) {
+    if (i && i->refs.fetch_sub(1) == 1) {
+        geometry_release(i->geometry);
+        delete i;
+    }
+}
+
+kf_scene_s* check_scene(kf_scene s) {
+    REQ(s != nullptr, "invalid scene handle");
+    return s;
+}
+kf_camera_s* check_camera(kf_camera c) {
+    REQ(c != nullptr, "invalid camera handle");
+    return c;
+}
+
+void material_to_table(const kf_material* m, uint32_t* idx) {
+    std::lock_guard<std::mutex> lk(global_mutex());
+    g_materials.push_back(*m);
+    ++g_material_version;
+    if (idx) *idx = (uint32_t)(g_materials.size() - 1);
+}
+
+void frame_reset(kf_renderer_s* r) { r->frame_count = -1; }
+
+void sync_stream(kf_renderer_s* r) {
+    if (!r->cfg.host_only) KF_CUDA_CHECK(cudaStreamSynchronize(r->stream));
+}
+
+} // namespace
+
+kf_scene_s::~kf_scene_s() {
+    for (kf_instance_s* i : instances) {
+        i->scene = nullptr;
+        instance_release(i);
+    }
+    for (kf_geometry_s* g : geometries) geometry_release(g);
+    for (kf_light_s* l : point_lights) delete l;
+    for (kf_light_s* l : active_lights) delete l;
+}
+
+kf_renderer_s::~kf_renderer_s() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    scenes.clear();
+    if (stream) cudaStreamDestroy(stream);
+}
+
+extern "C" {
+
+KF_API const char* kf_last_error(void) { return t_error.c_str(); }
+KF_API int kf_version(void) { return 10000; }
+
+KF_API void kf_config_init(kf_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->initial_width = 800;
+    c->initial_height = 600;
+    c->spp = 32;
+    c->path_depth = 8;
+    c->max_path_depth = 12;
+    c->russian_roulette = 1;
+    c->rr_min_bounces = 4;
+    c->nee = 1;
+    c->nee_min_bounces = 0;
+    c->accumulate_frames = 1;
+    c->use_denoiser = 0;
+    c->present = 1;
+    c->max_geometries = 128;
+    c->max_instances = 256;
+    c->max_textures = 128;
+    c->max_materials = 256;
+    c->seed = 0;
+    c->blas_leaf_size = 4;
+    c->tlas_leaf_size = 1;
+    c->max_paths_in_flight = 1ull << 24;
+    c->debug_outputs = 0;
+    c->profile = 0;
+    c->use_graph = 1;
+    c->device = 0;
+}
+
+KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
+    return guarded([&] {
+        REQ(out != nullptr, "out is null");
+        *out = nullptr;
+        auto r = std::make_unique<kf_renderer_s>();
+        if (cfg)
+            r->cfg = *cfg;
+        else
+            kf_config_init(&r->cfg);
+        if (!r->cfg.host_only) {
+            int ndev = 0;
+            cudaError_t e = cudaGetDeviceCount(&ndev);
+            KF_REQUIRE(e == cudaSuccess && ndev > 0, KF_ERR_NO_DEVICE,
+                       "no CUDA device available: the path tracer has no CPU fallback");
+            KF_REQUIRE((int)r->cfg.device < ndev, KF_ERR_NO_DEVICE, "requested CUDA device does not exist");
+            r->device = (int)r->cfg.device;
+            KF_CUDA_CHECK(cudaSetDevice(r->device));
+            KF_CUDA_CHECK(cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, r->device));
+            KF_CUDA_CHECK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+            for (cudaEvent_t& ev : r->ev) KF_CUDA_CHECK(cudaEventCreate(&ev));
+            upload_srgb_thresholds(srgb_threshold_table().data());
+        }
+        // persistent grids: enough resident warps to hide traversal latency
+        r->grid_extend = (uint32_t)r->num_sms * 16;
+        r->grid_shade = (uint32_t)r->num_sms * 8;
+        // Kuafu::Kuafu (kuafu.cpp:27-63): a scene with a 1x1 camera; present mode adds
+        // a camera of the initial size and makes it current.
+        kf_scene_s* s = new_scene(r.get());
+        r->current = s;
+        if (r->cfg.present) {
+            s->current_camera = scene_new_camera(s, r->cfg.initial_width, r->cfg.initial_height);
+        }
+        *out = r.release();
+    });
+}
+
+KF_API int kf_renderer_destroy(kf_renderer r) {
+    return guarded([&] {
+        if (!r) return;
+        if (!r->cfg.host_only) {
+            cudaSetDevice(r->device);
+            if (r->stream) cudaStreamSynchronize(r->stream);
+        }
+        delete r;
+    });
+}
+
+static void require_device(kf_renderer_s* r) {
+    KF_REQUIRE(!r->cfg.host_only, KF_ERR_NO_DEVICE,
+               "renderer was created host-only: rendering needs a CUDA device (there is no CPU fallback)");
+}
+
+KF_API int kf_renderer_get_config(kf_renderer r, kf_config* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        *out = r->cfg;
+    });
+}
+KF_API int kf_renderer_set_config(kf_renderer r, const kf_config* cfg) {
+    return guarded([&] {
+        REQ(r && cfg, "null argument");
+        const uint32_t dev = r->cfg.device;
+        r->cfg = *cfg;
+        r->cfg.device = dev;
+        // Config::setPathDepth clamps to the maximum (config.cpp:29-40, with the clamp
+        // immediately overwritten in kuafu; the value given is used as is).
+    });
+}
+KF_API int kf_renderer_get_scene(kf_renderer r, kf_scene* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        *out = r->current;
+    });
+}
+KF_API int kf_renderer_create_scene(kf_renderer r, kf_scene* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        *out = new_scene(r);
+    });
+}
+KF_API int kf_renderer_set_scene(kf_renderer r, kf_scene s) {
+    return guarded([&] {
+        REQ(r && s, "Trying to set an invalid scene!");
+        auto it = std::find_if(r->scenes.begin(), r->scenes.end(), [&](auto& p) { return p.get() == s; });
+        REQ(it != r->scenes.end(), "scene does not belong to this renderer");
+        if (r->current == s) return;
+        r->current = s;
+        frame_reset(r);
+    });
+}
+KF_API int kf_renderer_remove_scene(kf_renderer r, kf_scene s) {
+    return guarded([&] {
+        REQ(r && s, "Trying to remove an invalid scene!");
+        auto it = std::find_if(r->scenes.begin(), r->scenes.end(), [&](auto& p) { return p.get() == s; });
+        REQ(it != r->scenes.end(), "scene does not belong to this renderer");
+        sync_stream(r);
+        if (r->graph_exec) {
+            cudaGraphExecDestroy(r->graph_exec);
+            r->graph_exec = nullptr;
+            r->graph_key.clear();
+        }
+        if (r->current == s) r->current = nullptr;
+        r->scenes.erase(it);
+    });
+}
+KF_API int kf_renderer_is_running(kf_renderer r, int* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        *out = r->running ? 1 : 0;
+    });
+}
+
+KF_API int kf_renderer_run(kf_renderer r) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        KF_REQUIRE(r->current, KF_ERR_STATE, "no current scene");
+        kf_scene_s* s = r->current;
+        kf_camera_s* c = s->current_camera;
+        KF_REQUIRE(c, KF_ERR_STATE, "Trying to render with an invalid camera!");
+        require_device(r);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        // Camera::update (camera.cpp:41-51): a moved camera restarts accumulation
+        if (r->last_camera != c || std::memcmp(r->last_position, c->position, sizeof(r->last_position)) != 0) {
+            frame_reset(r);
+            r->last_camera = c;
+            std::memcpy(r->last_position, c->position, sizeof(r->last_position));
+        }
+        camera_update_view(c);
+        render_frame(r, s, c, r->cfg.spp);
+    });
+}
+
+KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint32_t count) {
+    return guarded([&] {
+        REQ(r && (items || count == 0), "null argument");
+        require_device(r);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        for (uint32_t i = 0; i < count; ++i) {
+            kf_scene_s* s = check_scene(items[i].scene);
+            kf_camera_s* c = check_camera(items[i].camera);
+            REQ(c->scene == s, "batch camera does not belong to its scene");
+            camera_update_view(c);
+            const int32_t saved = r->frame_count;
+            r->frame_count = -1; // batched views are independent single frames
+            render_frame(r, s, c, items[i].spp ? items[i].spp : r->cfg.spp);
+            r->frame_count = saved;
+        }
+    });
+}
+
+KF_API int kf_renderer_synchronize(kf_renderer r) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        sync_stream(r);
+    });
+}
+
+KF_API int kf_renderer_get_stream(kf_renderer r, void** out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        require_device(r);
+        *out = (void*)r->stream;
+    });
+}
+
+KF_API int kf_renderer_download_latest_frame(kf_renderer r, kf_camera cam, uint8_t* out, size_t bytes) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        require_device(r);
+        kf_camera_s* c = check_camera(cam);
+        KF_REQUIRE(c->has_frame, KF_ERR_STATE, "Invalid call to Camera::downloadLatestFrame");
+        const size_t need = (size_t)c->target_w * c->target_h * 4;
+        KF_REQUIRE(bytes >= need, KF_ERR_OUT_OF_RANGE, "output buffer too small for the frame");
+        KF_CUDA_CHECK(cudaMemcpyAsync(out, c->bgra.ptr, need, cudaMemcpyDeviceToHost, r->stream));
+        sync_stream(r);
+    });
+}
+
+KF_API int kf_renderer_download_aov(kf_renderer r, kf_camera cam, int kind, void* out, size_t bytes) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        require_device(r);
+        kf_camera_s* c = check_camera(cam);
+        KF_REQUIRE(c->has_frame, KF_ERR_STATE, "no frame rendered for this camera");
+        const size_t npix = (size_t)c->target_w * c->target_h;
+        const void* src = nullptr;
+        size_t need = 0;
+        switch (kind) {
+            case KF_AOV_RADIANCE_F32: src = c->accum.ptr; need = npix * 16; break;
+            case KF_AOV_ALBEDO_F32: src = c->albedo.ptr; need = npix * 16; break;
+            case KF_AOV_NORMAL_F32: src = c->normal.ptr; need = npix * 16; break;
+            case KF_AOV_DEPTH_F32: src = c->depth.ptr; need = npix * 4; break;
+            case KF_AOV_SUM_F64: src = c->sum64.ptr; need = npix * 32; break;
+            case KF_AOV_PATH_RADIANCE:
+                src = r->wave.radiance.ptr;
+                need = (size_t)r->stats.last_spp * npix * 16;
+                break;
+            case KF_AOV_PRIMARY_HITS:
+                KF_REQUIRE(r->cfg.debug_outputs, KF_ERR_STATE, "primary hits need debug_outputs = 1");
+                src = r->wave.primary.ptr;
+                need = (size_t)r->stats.last_spp * npix * sizeof(kf_hit);
+                break;
+            case KF_AOV_DENOISED_F32:
+                KF_REQUIRE(c->denoised.count == npix, KF_ERR_STATE, "no denoised frame for this camera");
+                src = c->denoised.ptr;
+                need = npix * 16;
+                break;
+            default: throw KfError(KF_ERR_INVALID_ARGUMENT, "unknown AOV kind");
+        }
+        KF_REQUIRE(bytes >= need, KF_ERR_OUT_OF_RANGE, "output buffer too small for the AOV");
+        KF_CUDA_CHECK(cudaMemcpyAsync(out, src, need, cudaMemcpyDeviceToHost, r->stream));
+        sync_stream(r);
+    });
+}
+
+KF_API int kf_renderer_get_stats(kf_renderer r, kf_stats* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        sync_stream(r);
+        if (r->wave.stats.count) {
+            unsigned long long h[16] = {};
+            KF_CUDA_CHECK(cudaMemcpy(h, r->wave.stats.ptr, sizeof(h), cudaMemcpyDeviceToHost));
+            r->stats.rays_primary = h[0];
+            r->stats.rays_extension = h[1];
+            r->stats.rays_shadow = h[2];
+            r->stats.node_visits = h[3];
+            r->stats.tri_tests = h[4];
+            r->stats.inst_visits = h[5];
+            r->stats.shadow_node_visits = h[6];
+            r->stats.shadow_tri_tests = h[7];
+            r->stats.shadow_inst_visits = h[8];
+        }
+        *out = r->stats;
+    });
+}
+KF_API int kf_renderer_reset_stats(kf_renderer r) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        sync_stream(r);
+        if (r->wave.stats.count && !r->cfg.host_only)
+            KF_CUDA_CHECK(cudaMemset(r->wave.stats.ptr, 0, r->wave.stats.bytes()));
+        const int32_t fc = r->stats.frame_count;
+        const uint32_t bn = r->stats.blas_nodes, tn = r->stats.tlas_nodes, ls = r->stats.last_spp;
+        std::memset(&r->stats, 0, sizeof(r->stats));
+        r->stats.frame_count = fc;
+        r->stats.blas_nodes = bn;
+        r->stats.tlas_nodes = tn;
+        r->stats.last_spp = ls;
+    });
+}
+KF_API int kf_renderer_count_traversal(kf_renderer r, int enable) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        r->count_traversal = enable != 0;
+    });
+}
+
+// ---- materials ----
+KF_API void kf_material_init(kf_material* m) {
+    if (!m) return;
+    std::memset(m, 0, sizeof(*m));
+    m->diffuse_color[0] = m->diffuse_color[1] = m->diffuse_color[2] = 1.0f;
+    m->alpha = 1.0f;
+    m->metallic = 0.0f;
+    m->specular = 0.5f;
+    m->roughness = 0.5f;
+    m->ior = 1.4f;
+    m->transmission = 0.0f;
+    m->emission[0] = m->emission[1] = m->emission[2] = 1.0f;
+    m->emission_strength = 0.0f;
+    m->diffuse_tex = m->metallic_tex = m->roughness_tex = m->transmission_tex = -1;
+}
+KF_API int kf_material_add(const kf_material* m, uint32_t* out_index) {
+    return guarded([&] {
+        REQ(m, "null material");
+        material_to_table(m, out_index);
+    });
+}
+KF_API uint32_t kf_material_count(void) {
+    std::lock_guard<std::mutex> lk(global_mutex());
+    return (uint32_t)g_materials.size();
+}
+KF_API int kf_material_get(uint32_t index, kf_material* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        std::lock_guard<std::mutex> lk(global_mutex());
+        KF_REQUIRE(index < g_materials.size(), KF_ERR_OUT_OF_RANGE, "material index out of range");
+        *out = g_materials[index];
+    });
+}
+KF_API int kf_material_clear(void) {
+    std::lock_guard<std::mutex> lk(global_mutex());
+    g_materials.clear();
+    ++g_material_version;
+    return KF_OK;
+}
+
+KF_API int kf_texture_create(const uint8_t* rgba8, uint32_t width, uint32_t height, int srgb, int32_t* out_id) {
+    return guarded([&] {
+        REQ(rgba8 && width && height && out_id, "invalid texture arguments");
+        std::lock_guard<std::mutex> lk(global_mutex());
+        HostTexture t;
+        t.w = width;
+        t.h = height;
+        t.srgb = srgb ? 1u : 0u;
+        t.rgba.assign(rgba8, rgba8 + (size_t)width * height * 4);
+        g_textures.push_back(std::move(t));
+        ++g_texture_version;
+        *out_id = (int32_t)(g_textures.size() - 1);
+    });
+}
+KF_API uint32_t kf_texture_count(void) {
+    std::lock_guard<std::mutex> lk(global_mutex());
+    return (uint32_t)g_textures.size();
+}
+
+// ---- geometry ----
+KF_API int kf_geometry_create(const kf_vertex* v, uint32_t nv, const uint32_t* idx, uint32_t nidx,
+                              const uint32_t* mat_index, uint32_t n_mat, kf_geometry* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        REQ(nidx % 3 == 0, "index count must be a multiple of 3");
+        REQ((v || nv == 0) && (idx || nidx == 0), "null vertex or index data");
+        REQ(n_mat >= nidx / 3, "matIndex must hold one entry per triangle");
+        for (uint32_t i = 0; i < nidx; ++i)
+            KF_REQUIRE(idx[i] < nv, KF_ERR_OUT_OF_RANGE, "vertex index out of range");
+        for (uint32_t i = 0; i < nv; ++i)
+            for (int k = 0; k < 3; ++k)
+                REQ(std::isfinite(v[i].pos[k]), "vertex position is not finite");
+        auto g = new kf_geometry_s();
+        g->vertices.assign(v, v + nv);
+        g->indices.assign(idx, idx + nidx);
+        g->mat_index.assign(mat_index, mat_index + n_mat);
+        *out = g;
+    });
+}
+KF_API int kf_geometry_set_material(kf_geometry g, const kf_material* m) {
+    return guarded([&] {
+        REQ(g && m, "null argument");
+        // Geometry::setMaterial (geometry.cpp:241-249)
+        g->opaque = m->alpha >= 1.0f;
+        uint32_t idx = 0;
+        material_to_table(m, &idx);
+        for (auto& x : g->mat_index) x = idx;
+        ++g->version;
+    });
+}
+KF_API int kf_geometry_set_flags(kf_geometry g, int opaque, int hide_render, int dynamic_) {
+    return guarded([&] {
+        REQ(g, "null geometry");
+        g->opaque = opaque != 0;
+        g->hide_render = hide_render != 0;
+        g->dynamic_ = dynamic_ != 0;
+        ++g->version;
+    });
+}
+KF_API int kf_geometry_recalculate_normals(kf_geometry g) {
+    return guarded([&] {
+        REQ(g, "null geometry");
+        recalculate_normals(g->vertices, g->indices);
+        ++g->version;
+    });
+}
+KF_API int kf_geometry_get_info(kf_geometry g, uint32_t* nv, uint32_t* ni) {
+    return guarded([&] {
+        REQ(g, "null geometry");
+        if (nv) *nv = (uint32_t)g->vertices.size();
+        if (ni) *ni = (uint32_t)g->indices.size();
+    });
+}
+KF_API int kf_geometry_get_data(kf_geometry g, kf_vertex* v, uint32_t* idx, uint32_t* mat) {
+    return guarded([&] {
+        REQ(g, "null geometry");
+        if (v) std::memcpy(v, g->vertices.data(), sizeof(kf_vertex) * g->vertices.size());
+        if (idx) std::memcpy(idx, g->indices.data(), sizeof(uint32_t) * g->indices.size());
+        if (mat) std::memcpy(mat, g->mat_index.data(), sizeof(uint32_t) * (g->indices.size() / 3));
+    });
+}
+KF_API int kf_geometry_release(kf_geometry g) {
+    return guarded([&] { geometry_release(g); });
+}
+KF_API int kf_geometry_create_builtin(int kind, float p0, float p1, const kf_material* m, kf_geometry* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        kf_material def;
+        kf_material_init(&def);
+        const kf_material* mm = m ? m : &def;
+        auto g = new kf_geometry_s();
+        try {
+            switch (kind) {
+                case KF_MESH_YZ_PLANE: mesh_yz_plane(g->vertices, g->indices); break;
+                case KF_MESH_CUBE: mesh_cube(g->vertices, g->indices); break;
+                case KF_MESH_SPHERE: mesh_sphere(g->vertices, g->indices); break;
+                case KF_MESH_CAPSULE: mesh_capsule(p0, p1, g->vertices, g->indices); break;
+                case KF_MESH_ICOSPHERE: mesh_icosphere((int)p0, g->vertices, g->indices); break;
+                default: throw KfError(KF_ERR_INVALID_ARGUMENT, "unknown builtin mesh kind");
+            }
+            // createX: isOpaque = alpha >= 1; matIndex = one fresh material for every index slot
+            g->opaque = mm->alpha >= 1.0f;
+            uint32_t idx = 0;
+            material_to_table(mm, &idx);
+            g->mat_index.assign(g->indices.size(), idx);
+            g->dynamic_ = true;
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+// ---- scene ----
+KF_API int kf_scene_submit_geometry(kf_scene s, kf_geometry g) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(g, "null geometry");
+        KF_REQUIRE(s->geometries.size() < s->renderer->cfg.max_geometries, KF_ERR_LIMIT,
+                   "Failed to submit geometry because geometries buffer size has been exceeded.");
+        geometry_retain(g);
+        s->geometries.push_back(g);
+        ++s->geom_stamp;
+    });
+}
+KF_API int kf_scene_clear_geometries(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        for (kf_instance_s* i : s->instances) {
+            i->scene = nullptr;
+            instance_release(i);
+        }
+        s->instances.clear();
+        for (kf_geometry_s* g : s->geometries) geometry_release(g);
+        s->geometries.clear();
+        ++s->geom_stamp;
+        ++s->inst_stamp;
+    });
+}
+KF_API int kf_scene_remove_geometry(kf_scene s, kf_geometry g) {
+    (void)s;
+    (void)g;
+    return fail(KF_ERR_NOT_IMPLEMENTED, "Not implemented!");
+}
+KF_API int kf_scene_submit_instance(kf_scene s, kf_geometry g, const float transform[16], kf_instance* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(g && transform, "null argument");
+        // Scene::submitGeometryInstance (scene.cpp:58-77)
+        KF_REQUIRE(s->instances.size() <= s->renderer->cfg.max_instances, KF_ERR_LIMIT,
+                   "Failed to submit geometry instance because instance buffer size has been exceeded.");
+        const bool known = std::find(s->geometries.begin(), s->geometries.end(), g) != s->geometries.end();
+        REQ(known, "Geometry not submitted!");
+        float rows[12];
+        affine_inverse_rows(transform, rows); // rejects singular transforms
+        auto in = new kf_instance_s();
+        in->geometry = g;
+        geometry_retain(g);
+        in->scene = s;
+        std::memcpy(in->transform, transform, sizeof(in->transform));
+        in->refs.store(out ? 2 : 1); // the scene's reference + the caller's handle
+        s->instances.push_back(in);
+        ++s->inst_stamp;
+        if (out) *out = in;
+    });
+}
+KF_API int kf_instance_set_transform(kf_instance i, const float transform[16]) {
+    return guarded([&] {
+        REQ(i && transform, "null argument");
+        float rows[12];
+        affine_inverse_rows(transform, rows);
+        std::memcpy(i->transform, transform, sizeof(i->transform));
+        if (i->scene) ++i->scene->inst_stamp;
+    });
+}
+KF_API int kf_scene_remove_instance(kf_scene s, kf_instance i) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(i, "Deleting an invalid geometry instance!");
+        auto it = std::find(s->instances.begin(), s->instances.end(), i);
+        if (it == s->instances.end()) return;
+        s->instances.erase(it);
+        i->scene = nullptr;
+        instance_release(i);
+        ++s->inst_stamp;
+    });
+}
+KF_API int kf_scene_clear_instances(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        for (kf_instance_s* i : s->instances) {
+            i->scene = nullptr;
+            instance_release(i);
+        }
+        s->instances.clear();
+        ++s->inst_stamp;
+    });
+}
+KF_API int kf_scene_instance_count(kf_scene s, uint32_t* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(out, "null argument");
+        *out = (uint32_t)s->instances.size();
+    });
+}
+KF_API int kf_scene_get_instance(kf_scene s, uint32_t index, kf_instance* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(out, "null argument");
+        KF_REQUIRE(index < s->instances.size(), KF_ERR_OUT_OF_RANGE, "Geometry Instances out of bound.");
+        *out = s->instances[index];
+    });
+}
+KF_API int kf_instance_release(kf_instance i) {
+    return guarded([&] { instance_release(i); });
+}
+KF_API int kf_scene_set_clear_color(kf_scene s, const float rgba[4]) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(rgba, "null argument");
+        std::memcpy(s->clear_color, rgba, sizeof(s->clear_color));
+        frame_reset(s->renderer); // Scene::setClearColor resets frameCount (scene.hpp:101-105)
+    });
+}
+KF_API int kf_scene_get_clear_color(kf_scene s, float rgba[4]) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(rgba, "null argument");
+        std::memcpy(rgba, s->clear_color, sizeof(s->clear_color));
+    });
+}
+KF_API int kf_scene_mark_geometries_changed(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        ++s->geom_stamp;
+    });
+}
+KF_API int kf_scene_mark_instances_changed(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        ++s->inst_stamp;
+    });
+}
+
+KF_API int kf_scene_set_directional_light(kf_scene s, const kf_directional_light* l) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(l, "null light");
+        s->dir_light = *l;
+        s->has_dir_light = true;
+    });
+}
+KF_API int kf_scene_remove_directional_light(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        s->has_dir_light = false;
+    });
+}
+KF_API int kf_scene_add_point_light(kf_scene s, const kf_point_light* l, kf_light* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(l, "null light");
+        if (out) *out = nullptr;
+        // Scene::addPointLight warns and drops lights past the limit (scene.hpp:159-164)
+        KF_REQUIRE(s->point_lights.size() < KF_MAX_POINT_LIGHTS, KF_ERR_LIMIT,
+                   "Reached max point light number. The light will not be added!");
+        auto L = new kf_light_s();
+        L->kind = 1;
+        L->point = *l;
+        L->scene = s;
+        s->point_lights.push_back(L);
+        if (out) *out = L;
+    });
+}
+KF_API int kf_scene_add_active_light(kf_scene s, const kf_active_light* l, kf_light* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(l, "null light");
+        if (out) *out = nullptr;
+        KF_REQUIRE(s->active_lights.size() < KF_MAX_ACTIVE_LIGHTS, KF_ERR_LIMIT,
+                   "Reached max active light number. The light will not be added!");
+        auto L = new kf_light_s();
+        L->kind = 2;
+        L->active = *l;
+        L->scene = s;
+        s->active_lights.push_back(L);
+        if (out) *out = L;
+    });
+}
+KF_API int kf_light_update_point(kf_light l, const kf_point_light* p) {
+    return guarded([&] {
+        REQ(l && p && l->kind == 1, "not a point light");
+        l->point = *p;
+    });
+}
+KF_API int kf_light_update_active(kf_light l, const kf_active_light* a) {
+    return guarded([&] {
+        REQ(l && a && l->kind == 2, "not an active light");
+        l->active = *a;
+    });
+}
+KF_API int kf_scene_remove_light(kf_scene s, kf_light l) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(l, "Deleting an invalid light!");
+        auto& v = l->kind == 1 ? s->point_lights : s->active_lights;
+        auto it = std::find(v.begin(), v.end(), l);
+        REQ(it != v.end(), "light does not belong to this scene");
+        v.erase(it);
+        delete l;
+    });
+}
+
+KF_API int kf_scene_create_camera(kf_scene s, int w, int h, kf_camera* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(out && w > 0 && h > 0, "invalid camera size");
+        *out = scene_new_camera(s, w, h);
+    });
+}
+KF_API int kf_scene_remove_camera(kf_scene s, kf_camera c) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(c, "Trying to remove an invalid camera!");
+        auto it = std::find_if(s->cameras.begin(), s->cameras.end(), [&](auto& p) { return p.get() == c; });
+        REQ(it != s->cameras.end(), "Trying to remove an camera which does not belong to the scene!");
+        kf_renderer_s* r = s->renderer;
+        sync_stream(r);
+        if (r->graph_exec) {
+            cudaGraphExecDestroy(r->graph_exec);
+            r->graph_exec = nullptr;
+            r->graph_key.clear();
+        }
+        if (s->current_camera == c) s->current_camera = nullptr;
+        if (r->last_camera == c) r->last_camera = nullptr;
+        s->cameras.erase(it);
+    });
+}
+KF_API int kf_scene_set_camera(kf_scene s, kf_camera c) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(c, "Trying to set an invalid camera!");
+        auto it = std::find_if(s->cameras.begin(), s->cameras.end(), [&](auto& p) { return p.get() == c; });
+        REQ(it != s->cameras.end(), "Trying to set a camera that does not belong to the scene!");
+        s->current_camera = c;
+    });
+}
+KF_API int kf_scene_get_camera(kf_scene s, kf_camera* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(out, "null argument");
+        *out = s->current_camera;
+    });
+}
+
+KF_API int kf_scene_export(kf_scene s, kf_flat_scene* out) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(out, "null argument");
+        std::memset(out, 0, sizeof(*out));
+        s->x_geoms.clear();
+        for (kf_geometry_s* g : s->geometries) {
+            kf_flat_geometry fg{};
+            fg.vertices = g->vertices.data();
+            fg.num_vertices = (uint32_t)g->vertices.size();
+            fg.num_triangles = (uint32_t)(g->indices.size() / 3);
+            fg.indices = g->indices.data();
+            fg.mat_index = g->mat_index.data();
+            fg.opaque = g->opaque ? 1u : 0u;
+            fg.hide_render = g->hide_render ? 1u : 0u;
+            s->x_geoms.push_back(fg);
+        }
+        s->x_insts.clear();
+        for (kf_instance_s* in : s->instances) {
+            kf_flat_instance fi{};
+            std::memcpy(fi.transform, in->transform, sizeof(fi.transform));
+            affine_inverse_rows(in->transform, fi.world_to_object);
+            size_t gi = 0;
+            for (; gi < s->geometries.size(); ++gi)
+                if (s->geometries[gi] == in->geometry) break;
+            fi.geometry_index = (uint32_t)gi;
+            s->x_insts.push_back(fi);
+        }
+        {
+            std::lock_guard<std::mutex> lk(global_mutex());
+            s->x_mats = flatten_materials();
+            s->x_texs.clear();
+            for (const HostTexture& t : g_textures) {
+                kf_texture_desc d{};
+                d.rgba8 = t.rgba.data();
+                d.width = t.w;
+                d.height = t.h;
+                d.srgb = t.srgb;
+                s->x_texs.push_back(d);
+            }
+        }
+        out->geometries = s->x_geoms.data();
+        out->num_geometries = (uint32_t)s->x_geoms.size();
+        out->instances = s->x_insts.data();
+        out->num_instances = (uint32_t)s->x_insts.size();
+        out->materials = s->x_mats.data();
+        out->num_materials = (uint32_t)s->x_mats.size();
+        out->textures = s->x_texs.data();
+        out->num_textures = (uint32_t)s->x_texs.size();
+        scene_light_ubos(s, &out->dlight, &out->plights, &out->alights);
+    });
+}
+
+// ---- camera ----
+KF_API int kf_camera_set_position(kf_camera c, const float p[3]) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(p, "null argument");
+        std::memcpy(c->position, p, sizeof(c->position));
+        camera_update_view(c);
+    });
+}
+KF_API int kf_camera_set_front(kf_camera c, const float f[3]) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(f, "null argument");
+        std::memcpy(c->front, f, sizeof(c->front));
+        camera_update_view(c);
+    });
+}
+KF_API int kf_camera_set_up(kf_camera c, const float u[3]) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(u, "null argument");
+        std::memcpy(c->up, u, sizeof(c->up));
+        camera_update_view(c);
+    });
+}
+KF_API int kf_camera_set_pose(kf_camera c, const float pose[16]) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(pose, "null argument");
+        // Camera::setPose (camera.cpp:131-139)
+        c->position[0] = pose[12]; c->position[1] = pose[13]; c->position[2] = pose[14];
+        c->front[0] = -pose[8]; c->front[1] = -pose[9]; c->front[2] = -pose[10];
+        c->up[0] = pose[4]; c->up[1] = pose[5]; c->up[2] = pose[6];
+        if (c->scene && c->scene->renderer) frame_reset(c->scene->renderer);
+    });
+}
+KF_API int kf_camera_get_pose(kf_camera c, float pose[16]) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(pose, "null argument");
+        // Camera::getPose (camera.cpp:32-39): columns front, -right, up, position
+        const float m[16] = {c->front[0],  c->front[1],  c->front[2],  0.0f, -c->right[0], -c->right[1],
+                             -c->right[2], 0.0f,         c->up[0],     c->up[1], c->up[2],  0.0f,
+                             c->position[0], c->position[1], c->position[2], 1.0f};
+        std::memcpy(pose, m, sizeof(m));
+    });
+}
+KF_API int kf_camera_set_full_perspective(kf_camera c, float w, float h, float fx, float fy, float cx, float cy,
+                                          float skew) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(w >= 1.0f && h >= 1.0f, "invalid image size");
+        c->width = (int)w;
+        c->height = (int)h;
+        c->fx = fx; c->fy = fy; c->cx = cx; c->cy = cy; c->skew = skew;
+        camera_update_proj(c);
+    });
+}
+KF_API int kf_camera_set_size(kf_camera c, int w, int h) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(w > 0 && h > 0, "invalid image size");
+        c->width = w;
+        c->height = h;
+        c->cx = (float)w / 2.0f;
+        c->cy = (float)h / 2.0f;
+        camera_update_proj(c);
+    });
+}
+KF_API int kf_camera_reset_view(kf_camera c) {
+    return guarded([&] {
+        check_camera(c);
+        c->position[0] = c->position[1] = c->position[2] = 0.0f;
+        const float up[3] = {0, 0, 1}, right[3] = {0, -1, 0}, front[3] = {1, 0, 0};
+        std::memcpy(c->up, up, sizeof(up));
+        std::memcpy(c->right, right, sizeof(right));
+        std::memcpy(c->front, front, sizeof(front));
+        camera_update_view(c);
+        if (c->scene && c->scene->renderer) frame_reset(c->scene->renderer);
+    });
+}
+KF_API int kf_camera_get_size(kf_camera c, int* w, int* h) {
+    return guarded([&] {
+        check_camera(c);
+        if (w) *w = c->width;
+        if (h) *h = c->height;
+    });
+}
+KF_API int kf_camera_get_ubo(kf_camera c, kf_camera_ubo* out) {
+    return guarded([&] {
+        check_camera(c);
+        REQ(out, "null argument");
+        camera_update_view(c);
+        camera_ubo(c, out);
+    });
+}
+
+KF_API int kf_relmse(kf_renderer r, const float* x, const float* ref, uint64_t n, double eps, double* out) {
+    return guarded([&] {
+        REQ(r && x && ref && out, "null argument");
+        require_device(r);
+        const uint32_t blocks = (uint32_t)std::max(1, std::min(r->num_sms * 4, (int)((n + 255) / 256)));
+        if (r->scratch64.count < (size_t)blocks + 1) r->scratch64.resize(blocks + 1, r->stream);
+        launch_relmse(reinterpret_cast<const float4*>(x), reinterpret_cast<const float4*>(ref), n, eps,
+                      r->scratch64.ptr, blocks, r->scratch64.ptr + blocks, r->stream);
+        KF_CUDA_CHECK(cudaMemcpyAsync(out, r->scratch64.ptr + blocks, sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+        sync_stream(r);
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,403 @@
+// kf_scene.cu — scene flattening and acceleration-structure upkeep.
+//
+// Mirrors kuafu's Scene::uploadGeometries / uploadGeometryInstances /
+// uploadLightBuffers (src/core/scene.cpp:252-467) and the BLAS/TLAS management
+// of RayTracer (src/core/rt/rt.cpp:142-495), with the driver's builder replaced
+// by the GPU LBVH of kf_bvh.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "kf_bvh.h"
+#include "kf_host.h"
+
+namespace kf {
+
+std::mutex& global_mutex();
+extern std::vector<kf_material> g_materials;
+extern std::vector<HostTexture> g_textures;
+extern uint64_t g_material_version, g_texture_version;
+
+namespace {
+
+// Triangle boxes of one geometry (object space).
+__global__ void k_tri_boxes(const float4* __restrict__ verts, const uint32_t* __restrict__ idx, uint32_t vbase,
+                            uint32_t tbase, uint32_t n, float4* lo, float4* hi) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float4 p[3];
+    for (int k = 0; k < 3; ++k) p[k] = verts[3 * (size_t)(vbase + idx[3 * (size_t)(tbase + t) + k])];
+    lo[t] = make_float4(fminf(fminf(p[0].x, p[1].x), p[2].x), fminf(fminf(p[0].y, p[1].y), p[2].y),
+                        fminf(fminf(p[0].z, p[1].z), p[2].z), 0.0f);
+    hi[t] = make_float4(fmaxf(fmaxf(p[0].x, p[1].x), p[2].x), fmaxf(fmaxf(p[0].y, p[1].y), p[2].y),
+                        fmaxf(fmaxf(p[0].z, p[1].z), p[2].z), 0.0f);
+}
+
+// Precomputed triangles in BVH leaf order; the primitive id rides in v0.w.
+__global__ void k_tri_gather(const float4* __restrict__ verts, const uint32_t* __restrict__ idx,
+                             const uint32_t* __restrict__ order, uint32_t vbase, uint32_t tbase, uint32_t n, Tri* out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t prim = order[j];
+    float4 p[3];
+    for (int k = 0; k < 3; ++k) p[k] = verts[3 * (size_t)(vbase + idx[3 * (size_t)(tbase + prim) + k])];
+    Tri t;
+    t.v0 = make_float4(p[0].x, p[0].y, p[0].z, __uint_as_float(prim));
+    t.v1 = make_float4(p[1].x, p[1].y, p[1].z, 0.0f);
+    t.v2 = make_float4(p[2].x, p[2].y, p[2].z, 0.0f);
+    out[j] = t;
+}
+
+// Rebase a freshly built node array into a pool: inner children += node_base,
+// leaf children += leaf_base.
+__global__ void k_rebase(const Node4* __restrict__ in, uint32_t n, uint32_t node_base, uint32_t leaf_base, Node4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Node4 o = in[i];
+    int c[4] = {o.child.x, o.child.y, o.child.z, o.child.w};
+    const int k[4] = {o.cnt.x, o.cnt.y, o.cnt.z, o.cnt.w};
+    for (int q = 0; q < 4; ++q) {
+        if (k[q] == 0) c[q] += (int)node_base;
+        else if (k[q] > 0) c[q] += (int)leaf_base;
+    }
+    o.child = make_int4(c[0], c[1], c[2], c[3]);
+    out[i] = o;
+}
+
+__global__ void k_map_ids(const uint32_t* __restrict__ order, const uint32_t* __restrict__ ids, uint32_t n,
+                          uint32_t* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = ids[order[i]];
+}
+
+void root_box(const Node4& n, std::array<float, 6>& b) {
+    const float lx[4] = {n.lox.x, n.lox.y, n.lox.z, n.lox.w}, hx[4] = {n.hix.x, n.hix.y, n.hix.z, n.hix.w};
+    const float ly[4] = {n.loy.x, n.loy.y, n.loy.z, n.loy.w}, hy[4] = {n.hiy.x, n.hiy.y, n.hiy.z, n.hiy.w};
+    const float lz[4] = {n.loz.x, n.loz.y, n.loz.z, n.loz.w}, hz[4] = {n.hiz.x, n.hiz.y, n.hiz.z, n.hiz.w};
+    const int cn[4] = {n.cnt.x, n.cnt.y, n.cnt.z, n.cnt.w};
+    b = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 4; ++c) {
+        if (cn[c] < 0) continue;
+        b[0] = std::min(b[0], lx[c]); b[1] = std::min(b[1], ly[c]); b[2] = std::min(b[2], lz[c]);
+        b[3] = std::max(b[3], hx[c]); b[4] = std::max(b[4], hy[c]); b[5] = std::max(b[5], hz[c]);
+    }
+}
+
+} // namespace
+
+// Light uniform buffers exactly as Scene::uploadLightBuffers builds them (scene.cpp:252-292).
+void scene_light_ubos(const kf_scene_s* s, kf_dir_light_ubo* d, kf_point_lights_ubo* p, kf_active_lights_ubo* a) {
+    std::memset(d, 0, sizeof(*d));
+    std::memset(p, 0, sizeof(*p));
+    std::memset(a, 0, sizeof(*a));
+    if (s->has_dir_light) {
+        const float* dir = s->dir_light.direction;
+        // glm::normalize: v * inversesqrt(dot(v, v))
+        const float len2 = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+        const float inv = 1.0f / std::sqrt(len2);
+        d->direction[0] = dir[0] * inv;
+        d->direction[1] = dir[1] * inv;
+        d->direction[2] = dir[2] * inv;
+        d->direction[3] = s->dir_light.softness;
+        d->rgbs[0] = s->dir_light.color[0];
+        d->rgbs[1] = s->dir_light.color[1];
+        d->rgbs[2] = s->dir_light.color[2];
+        d->rgbs[3] = s->dir_light.strength;
+    } else {
+        d->rgbs[3] = 0.0f;
+    }
+    for (size_t i = 0; i < KF_MAX_POINT_LIGHTS; ++i) {
+        if (i < s->point_lights.size()) {
+            const kf_point_light& l = s->point_lights[i]->point;
+            p->posr[i][0] = l.position[0]; p->posr[i][1] = l.position[1]; p->posr[i][2] = l.position[2];
+            p->posr[i][3] = l.radius;
+            p->rgbs[i][0] = l.color[0]; p->rgbs[i][1] = l.color[1]; p->rgbs[i][2] = l.color[2];
+            p->rgbs[i][3] = l.strength;
+        } else {
+            p->rgbs[i][3] = 0.0f;
+        }
+    }
+    for (size_t i = 0; i < KF_MAX_ACTIVE_LIGHTS; ++i) {
+        if (i < s->active_lights.size()) {
+            const kf_active_light& l = s->active_lights[i]->active;
+            float vinv[16];
+            inverse4_d(l.view, vinv);
+            std::memcpy(a->view[i], l.view, sizeof(float) * 16);
+            perspective(l.fov, 1.0f, 0.01f, 1000.0f, a->proj[i]);
+            a->front[i][0] = -vinv[2 * 4 + 0]; a->front[i][1] = -vinv[2 * 4 + 1]; a->front[i][2] = -vinv[2 * 4 + 2];
+            a->front[i][3] = 1.0f;
+            a->rgbs[i][0] = l.color[0]; a->rgbs[i][1] = l.color[1]; a->rgbs[i][2] = l.color[2];
+            a->rgbs[i][3] = l.strength;
+            a->position[i][0] = vinv[3 * 4 + 0]; a->position[i][1] = vinv[3 * 4 + 1];
+            a->position[i][2] = vinv[3 * 4 + 2]; a->position[i][3] = 0.0f;
+            const int tex = (l.tex_id >= 0 && (uint32_t)l.tex_id < g_textures.size()) ? l.tex_id : -1;
+            a->sftp[i][0] = l.softness; a->sftp[i][1] = l.fov; a->sftp[i][2] = (float)tex; a->sftp[i][3] = 0.0f;
+        } else {
+            a->front[i][3] = 0.0f;
+        }
+    }
+}
+
+std::vector<kf_material_gpu> flatten_materials() {
+    std::vector<kf_material_gpu> out;
+    out.reserve(g_materials.size());
+    for (const kf_material& m : g_materials) {
+        kf_material_gpu g{};
+        g.diffuse[0] = m.diffuse_color[0]; g.diffuse[1] = m.diffuse_color[1]; g.diffuse[2] = m.diffuse_color[2];
+        g.diffuse[3] = 0.0f;
+        g.emission[0] = m.emission[0]; g.emission[1] = m.emission[1]; g.emission[2] = m.emission[2];
+        g.emission[3] = m.emission_strength;
+        g.alpha = m.alpha; g.metallic = m.metallic; g.specular = m.specular; g.roughness = m.roughness;
+        g.ior = m.ior; g.transmission = m.transmission;
+        auto tex = [](int32_t id) { return (id >= 0 && (size_t)id < g_textures.size()) ? id : -1; };
+        g.diffuse_tex = tex(m.diffuse_tex);
+        g.metallic_tex = tex(m.metallic_tex);
+        g.roughness_tex = tex(m.roughness_tex);
+        g.transmission_tex = tex(m.transmission_tex);
+        out.push_back(g);
+    }
+    return out;
+}
+
+// Bring the device copy of a scene up to date: geometry buffers + BLAS when the
+// geometry set changed, TLAS when instances changed, materials / textures when the
+// global tables changed, lights every frame (uploadLightBuffers runs every frame).
+void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
+    cudaStream_t st = r->stream;
+    SceneGpu& G = s->gpu;
+    bool rebuilt_geom = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool timing = true;
+    if (timing) {
+        KF_CUDA_CHECK(cudaEventCreate(&e0));
+        KF_CUDA_CHECK(cudaEventCreate(&e1));
+        KF_CUDA_CHECK(cudaEventRecord(e0, st));
+    }
+    bool built_any = false;
+    if (G.built_geom_stamp != s->geom_stamp) {
+        built_any = true;
+        rebuilt_geom = true;
+        const size_t ng = s->geometries.size();
+        std::vector<float4> verts;
+        std::vector<uint32_t> idx, mat;
+        std::vector<uint4> geom(ng);
+        G.vert_offset.assign(ng, 0);
+        G.tri_offset.assign(ng, 0);
+        size_t nv = 0, nt = 0;
+        for (size_t gi = 0; gi < ng; ++gi) {
+            nv += s->geometries[gi]->vertices.size();
+            nt += s->geometries[gi]->indices.size() / 3;
+        }
+        verts.resize(nv * 3);
+        idx.reserve(nt * 3);
+        mat.reserve(nt);
+        size_t vo = 0, to = 0;
+        for (size_t gi = 0; gi < ng; ++gi) {
+            const kf_geometry_s* g = s->geometries[gi];
+            const uint32_t ntri = (uint32_t)(g->indices.size() / 3);
+            std::memcpy(&verts[vo * 3], g->vertices.data(), sizeof(kf_vertex) * g->vertices.size());
+            idx.insert(idx.end(), g->indices.begin(), g->indices.begin() + 3 * (size_t)ntri);
+            mat.insert(mat.end(), g->mat_index.begin(), g->mat_index.begin() + ntri);
+            uint32_t flags = (g->opaque ? 1u : 0u) | (g->hide_render ? 2u : 0u);
+            geom[gi] = make_uint4((uint32_t)vo, (uint32_t)to, ntri, flags);
+            G.vert_offset[gi] = (uint32_t)vo;
+            G.tri_offset[gi] = (uint32_t)to;
+            vo += g->vertices.size();
+            to += ntri;
+        }
+        G.verts.upload(verts.data(), verts.size(), st);
+        G.indices.upload(idx.data(), idx.size(), st);
+        G.matidx.upload(mat.data(), mat.size(), st);
+        G.geom.upload(geom.data(), geom.size(), st);
+
+        // BLAS per geometry, appended to one node pool and one triangle pool.
+        std::vector<Node4> pool_host; // not used: pools are assembled on device
+        G.blas_root.assign(ng, 0);
+        G.blas_box.assign(ng, {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY});
+        size_t total_nodes_est = 0;
+        for (size_t gi = 0; gi < ng; ++gi) total_nodes_est += std::max<size_t>(1, s->geometries[gi]->indices.size() / 3);
+        G.blas_nodes.resize(std::max<size_t>(total_nodes_est, 1), st);
+        G.tris.resize(std::max<size_t>(nt, 1), st);
+        uint32_t node_base = 0;
+        DeviceBuffer<float4> lo, hi;
+        DeviceBuffer<Node4> nodes;
+        DeviceBuffer<uint32_t> order;
+        for (size_t gi = 0; gi < ng; ++gi) {
+            const uint32_t ntri = geom[gi].z;
+            if (ntri == 0) continue;
+            lo.resize(ntri, st);
+            hi.resize(ntri, st);
+            k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, geom[gi].x, geom[gi].y, ntri,
+                                                            lo.ptr, hi.ptr);
+            KF_CUDA_CHECK(cudaGetLastError());
+            const int nn = build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes,
+                                          order, st);
+            k_tri_gather<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, order.ptr, geom[gi].x,
+                                                             geom[gi].y, ntri, G.tris.ptr + geom[gi].y);
+            k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y,
+                                                       G.blas_nodes.ptr + node_base);
+            KF_CUDA_CHECK(cudaGetLastError());
+            Node4 root;
+            KF_CUDA_CHECK(cudaMemcpyAsync(&root, nodes.ptr, sizeof(Node4), cudaMemcpyDeviceToHost, st));
+            KF_CUDA_CHECK(cudaStreamSynchronize(st));
+            root_box(root, G.blas_box[gi]);
+            G.blas_root[gi] = node_base;
+            node_base += (uint32_t)nn;
+        }
+        G.blas_node_count = node_base;
+        G.built_geom_stamp = s->geom_stamp;
+    }
+    if (G.built_material_version != g_material_version || rebuilt_geom) {
+        std::vector<kf_material_gpu> mats = flatten_materials();
+        if (mats.empty()) mats.push_back(kf_material_gpu{});
+        G.materials.upload(mats.data(), mats.size(), st);
+        G.built_material_version = g_material_version;
+    }
+    if (G.built_texture_version != g_texture_version || G.srgb_decode.count == 0) {
+        std::vector<uint4> info;
+        std::vector<uchar4> texels;
+        for (const HostTexture& t : g_textures) {
+            info.push_back(make_uint4((uint32_t)texels.size(), t.w, t.h, t.srgb));
+            const uchar4* p = reinterpret_cast<const uchar4*>(t.rgba.data());
+            texels.insert(texels.end(), p, p + (size_t)t.w * t.h);
+        }
+        if (info.empty()) info.push_back(make_uint4(0, 1, 1, 0));
+        if (texels.empty()) texels.push_back(make_uchar4(255, 255, 255, 255));
+        G.tex_info.upload(info.data(), info.size(), st);
+        G.texels.upload(texels.data(), texels.size(), st);
+        const std::vector<float>& dec = srgb_decode_table();
+        G.srgb_decode.upload(dec.data(), dec.size(), st);
+        G.built_texture_version = g_texture_version;
+    }
+    if (rebuilt_geom || G.built_inst_stamp != s->inst_stamp) {
+        built_any = true;
+        const size_t ni = s->instances.size();
+        std::vector<InstanceRec> recs(ni);
+        std::vector<float4> blo, bhi;
+        std::vector<uint32_t> ids;
+        for (size_t i = 0; i < ni; ++i) {
+            const kf_instance_s* in = s->instances[i];
+            size_t gi = 0;
+            for (; gi < s->geometries.size(); ++gi)
+                if (s->geometries[gi] == in->geometry) break;
+            KF_REQUIRE(gi < s->geometries.size(), KF_ERR_STATE, "instance references a geometry not submitted to the scene");
+            float rows[12];
+            affine_inverse_rows(in->transform, rows);
+            InstanceRec& rc = recs[i];
+            rc.w2o0 = make_float4(rows[0], rows[1], rows[2], rows[3]);
+            rc.w2o1 = make_float4(rows[4], rows[5], rows[6], rows[7]);
+            rc.w2o2 = make_float4(rows[8], rows[9], rows[10], rows[11]);
+            rc.blas_root = G.blas_root.empty() ? 0 : G.blas_root[gi];
+            rc.geometry = (uint32_t)gi;
+            const kf_geometry_s* g = s->geometries[gi];
+            const bool hidden = g->hide_render || g->indices.size() < 3;
+            rc.flags = (g->opaque ? 1u : 0u) | (hidden ? 2u : 0u);
+            rc.pad = 0;
+            if (hidden) continue;
+            // world box of the 8 transformed corners of the BLAS box (double), padded
+            const std::array<float, 6>& b = G.blas_box[gi];
+            double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+            const float* m = in->transform;
+            for (int c = 0; c < 8; ++c) {
+                const double p[3] = {(c & 1) ? b[3] : b[0], (c & 2) ? b[4] : b[1], (c & 4) ? b[5] : b[2]};
+                for (int k = 0; k < 3; ++k) {
+                    const double v = (double)m[0 * 4 + k] * p[0] + (double)m[1 * 4 + k] * p[1] +
+                                     (double)m[2 * 4 + k] * p[2] + (double)m[3 * 4 + k];
+                    mn[k] = std::min(mn[k], v);
+                    mx[k] = std::max(mx[k], v);
+                }
+            }
+            double mag = 0.0;
+            for (int k = 0; k < 3; ++k) mag = std::max(mag, std::max(std::fabs(mn[k]), std::fabs(mx[k])));
+            const double pad = mag * 0x1.0p-16 + 1e-6;
+            blo.push_back(make_float4((float)(mn[0] - pad), (float)(mn[1] - pad), (float)(mn[2] - pad), 0.0f));
+            bhi.push_back(make_float4((float)(mx[0] + pad), (float)(mx[1] + pad), (float)(mx[2] + pad), 0.0f));
+            ids.push_back((uint32_t)i);
+        }
+        G.inst.upload(recs.data(), std::max<size_t>(recs.size(), 0), st);
+        if (recs.empty()) G.inst.resize(1, st);
+        const uint32_t nv = (uint32_t)ids.size();
+        if (nv > 0) {
+            DeviceBuffer<float4> dlo, dhi;
+            DeviceBuffer<uint32_t> dids, order;
+            dlo.upload(blo.data(), nv, st);
+            dhi.upload(bhi.data(), nv, st);
+            dids.upload(ids.data(), nv, st);
+            const int nn = build_wide_bvh(dlo.ptr, dhi.ptr, (int)nv, (int)std::max(1u, r->cfg.tlas_leaf_size),
+                                          G.tlas_nodes, order, st);
+            G.tlas_inst.resize(nv, st);
+            k_map_ids<<<(nv + 255) / 256, 256, 0, st>>>(order.ptr, dids.ptr, nv, G.tlas_inst.ptr);
+            KF_CUDA_CHECK(cudaGetLastError());
+            KF_CUDA_CHECK(cudaStreamSynchronize(st));
+            G.tlas_node_count = (uint32_t)nn;
+        } else {
+            G.tlas_node_count = 0;
+            G.tlas_nodes.resize(1, st);
+            G.tlas_inst.resize(1, st);
+        }
+        G.built_inst_stamp = s->inst_stamp;
+    }
+    if (timing) {
+        KF_CUDA_CHECK(cudaEventRecord(e1, st));
+        KF_CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        if (built_any) r->stats.bvh_build_ms += ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    // lights: every frame, like uploadUniformBuffers
+    kf_dir_light_ubo d;
+    kf_point_lights_ubo p;
+    kf_active_lights_ubo a;
+    scene_light_ubos(s, &d, &p, &a);
+    G.dlight.upload(&d, 1, st);
+    G.plights.upload(&p, 1, st);
+    G.alights.upload(&a, 1, st);
+
+    SceneDev& v = G.view;
+    v.verts = G.verts.ptr;
+    v.indices = G.indices.ptr;
+    v.matidx = G.matidx.ptr;
+    v.geom = G.geom.ptr;
+    v.materials = G.materials.ptr;
+    v.inst = G.inst.ptr;
+    v.blas_nodes = G.blas_nodes.ptr;
+    v.tris = G.tris.ptr;
+    v.tlas_nodes = G.tlas_nodes.ptr;
+    v.tlas_inst = G.tlas_inst.ptr;
+    v.dlight = G.dlight.ptr;
+    v.plights = G.plights.ptr;
+    v.alights = G.alights.ptr;
+    v.tex_info = G.tex_info.ptr;
+    v.texels = G.texels.ptr;
+    v.srgb_decode = G.srgb_decode.ptr;
+    v.num_instances = (uint32_t)s->instances.size();
+    v.has_tlas = G.tlas_node_count > 0 ? 1u : 0u;
+    v.num_textures = (uint32_t)g_textures.size();
+    // light slots in the order the shaders sum them: directional, points, actives
+    uint32_t ns = 0;
+    if (d.rgbs[3] != 0.0f) {
+        v.slot_group[ns] = 0;
+        v.slot_index[ns] = 0;
+        ++ns;
+    }
+    for (uint32_t i = 0; i < KF_MAX_POINT_LIGHTS; ++i)
+        if (p.rgbs[i][3] > 0.0f) {
+            v.slot_group[ns] = 1;
+            v.slot_index[ns] = (uint8_t)i;
+            ++ns;
+        }
+    for (uint32_t i = 0; i < KF_MAX_ACTIVE_LIGHTS; ++i)
+        if (a.front[i][3] > 0.0f) {
+            v.slot_group[ns] = 2;
+            v.slot_index[ns] = (uint8_t)i;
+            ++ns;
+        }
+    v.num_slots = ns;
+    r->stats.blas_nodes = G.blas_node_count;
+    r->stats.tlas_nodes = G.tlas_node_count;
+}
+
+} // namespace kf

@@ -1,0 +1,943 @@
+// kf_wavefront.cu — the wavefront path tracer that replaces kuafu's single
+// ray-tracing pipeline launch (src/core/rt/rt.cpp:637-666) and its shaders
+// (resources/shaders/PathTrace.{rgen,rchit,rahit,rmiss}, PathTraceShadow.rmiss).
+//
+// One frame = every (pixel, sample) path of a camera, processed bounce by bounce:
+//   raygen   camera rays                                  (PathTrace.rgen:30-75)
+//   extend   closest hit, two-level BVH4 traversal         (traceRayEXT, rgen:97-107)
+//   shade    miss / emission / PrincipledBSDF sampling,    (PathTrace.rmiss, rchit:322-468)
+//            light samples -> shadow queue, RR             (rchit:204-316, rgen:109-138)
+//   shadow   any-hit occlusion of the shadow queue         (rchit:175-200)
+//   gather   ordered NEE sum into the path radiance        (rchit:457-460, rgen:111)
+// then a per-pixel resolve (rgen:140-166) and the sRGB frame (PostProcessing.frag).
+// Queues are compacted with warp ballots + one atomic per warp.
+//
+// This file is compiled with -fmad=false: float expressions round exactly as
+// written, matching the CPU oracle operation for operation.
+#include "kf_wavefront.h"
+
+#include "kf_util.h"
+
+namespace kf {
+
+namespace {
+
+constexpr uint32_t kMiss = 0xFFFFFFFFu;
+constexpr int kStack = 96;
+constexpr uint32_t kInstTag = 0x80000000u;
+constexpr uint32_t kPopTag = 0xC0000000u;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+struct HitOut {
+    float t, u, v;
+    uint32_t inst, prim;
+};
+
+struct TraceCounters {
+    uint32_t nodes, tris, insts;
+};
+
+// Two-level traversal. SHADOW: any hit in [tmin, tmax] terminates (gl_RayFlags
+// TerminateOnFirstHit | Opaque | SkipClosestHitShader, rchit:182-184).
+// Stochastic alpha of non-opaque geometry (PathTrace.rahit:30-48): a candidate is
+// ignored when alpha == 0 or when a uniform draw exceeds alpha. The draws come from
+// the path's any-hit stream; their order follows the traversal order.
+struct AnyHitCtx {
+    const PathKey* pk;
+    Stream st;
+};
+
+__device__ __forceinline__ bool anyhit_accept(const SceneDev& s, uint32_t geometry, uint32_t prim, AnyHitCtx& ah) {
+    const uint4 gi = __ldg(s.geom + geometry);
+    const float alpha = s.materials[__ldg(s.matidx + gi.y + prim)].alpha;
+    if (alpha == 0.0f) return false;
+    if (ah.pk && ah.st.next(*ah.pk) > alpha) return false;
+    return true;
+}
+
+template <bool SHADOW, bool COUNT>
+__device__ bool trace(const SceneDev& s, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
+                      float tmax, HitOut& h, TraceCounters& cnt, AnyHitCtx* ah = nullptr) {
+    h.inst = kMiss;
+    h.t = h.u = h.v = 0.0f;
+    h.prim = 0;
+    if (!s.has_tlas) return false;
+    PRay wr;
+    wr.ox = ox; wr.oy = oy; wr.oz = oz;
+    wr.dx = dx; wr.dy = dy; wr.dz = dz;
+    prep_ray(wr);
+    PRay r = wr;
+    uint32_t stack[kStack];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool in_blas = false;
+    uint32_t cur_inst = 0;
+    uint32_t cur_geom = 0;
+    bool cur_opaque = true;
+    float best = tmax;
+    while (sp > 0) {
+        const uint32_t e = stack[--sp];
+        if (e == kPopTag) {
+            in_blas = false;
+            r = wr;
+            continue;
+        }
+        if (e & kInstTag) {
+            cur_inst = e & ~kInstTag;
+            const InstanceRec* ip = s.inst + cur_inst;
+            InstanceRec in;
+            in.w2o0 = __ldg(&ip->w2o0);
+            in.w2o1 = __ldg(&ip->w2o1);
+            in.w2o2 = __ldg(&ip->w2o2);
+            const uint4 meta = __ldg(reinterpret_cast<const uint4*>(ip) + 3);
+            if (COUNT) cnt.insts++;
+            if (meta.z & 2u) continue; // hidden (dummy BLAS, rt.cpp:156)
+            cur_geom = meta.y;
+            cur_opaque = (meta.z & 1u) != 0;
+            to_object(in, wr.ox, wr.oy, wr.oz, wr.dx, wr.dy, wr.dz, r);
+            in_blas = true;
+            if (sp + 2 > kStack) continue;
+            stack[sp++] = kPopTag;
+            stack[sp++] = meta.x;
+            continue;
+        }
+        const Node4 n = load_node(in_blas ? s.blas_nodes : s.tlas_nodes, e);
+        if (COUNT) cnt.nodes++;
+        float tn[4];
+        const int mask = box4(r, n, tmin, best, tn);
+        uint32_t ic[4];
+        float it[4];
+        int k = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (!(mask & (1 << c))) continue;
+            const int cn = lanei(n.cnt, c);
+            const int ch = lanei(n.child, c);
+            if (cn == 0) {
+                ic[k] = (uint32_t)ch;
+                it[k] = tn[c];
+                ++k;
+            } else if (cn > 0) {
+                if (in_blas) {
+                    for (int q = 0; q < cn; ++q) {
+                        const float4* tp = reinterpret_cast<const float4*>(s.tris + ch + q);
+                        const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                        if (COUNT) cnt.tris++;
+                        float t, u, v;
+                        if (!intersect_tri(r, a, b, cc, tmin, best, t, u, v)) continue;
+                        const uint32_t prim = __float_as_uint(a.w);
+                        if (SHADOW) {
+                            h.inst = cur_inst;
+                            return true;
+                        }
+                        if (!closer(t, cur_inst, prim, h.t, h.inst, h.prim)) continue;
+                        if (!cur_opaque && ah && !anyhit_accept(s, cur_geom, prim, *ah)) continue;
+                        h.t = t; h.u = u; h.v = v; h.inst = cur_inst; h.prim = prim;
+                        best = t;
+                    }
+                } else {
+                    for (int q = 0; q < cn; ++q) {
+                        if (sp < kStack) stack[sp++] = kInstTag | __ldg(s.tlas_inst + ch + q);
+                    }
+                }
+            }
+        }
+        // push inner children far-to-near so the nearest is popped first
+        for (int a = 1; a < k; ++a) {
+            const float tv = it[a];
+            const uint32_t cv = ic[a];
+            int b = a - 1;
+            while (b >= 0 && it[b] < tv) {
+                it[b + 1] = it[b];
+                ic[b + 1] = ic[b];
+                --b;
+            }
+            it[b + 1] = tv;
+            ic[b + 1] = cv;
+        }
+        for (int a = 0; a < k; ++a)
+            if (sp < kStack) stack[sp++] = ic[a];
+    }
+    return h.inst != kMiss;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// Warp-aggregated append: one atomic per warp, positions by ballot prefix.
+// Must be reached by all 32 lanes (warp-uniform control flow).
+__device__ __forceinline__ uint32_t warp_append(bool pred, uint32_t* counter) {
+    const uint32_t m = __ballot_sync(kFull, pred);
+    uint32_t base = 0;
+    if (m) {
+        if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, (uint32_t)__popc(m));
+        base = __shfl_sync(kFull, base, 0);
+    }
+    return base + __popc(m & lanemask_lt());
+}
+
+__device__ __forceinline__ void warp_add_stat(unsigned long long* p, uint32_t v) {
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, (unsigned long long)v);
+}
+
+// mat4 (column-major) * vec4, columns summed in order.
+__device__ __forceinline__ void mat4_mul(const float* m, const float v[4], float out[4]) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) out[r] = m[0 * 4 + r] * v[0] + m[1 * 4 + r] * v[1] + m[2 * 4 + r] * v[2] + m[3 * 4 + r] * v[3];
+}
+
+// ---------------------------------------------------------------------------
+// Ray generation (PathTrace.rgen:30-75).
+// ---------------------------------------------------------------------------
+__global__ void k_raygen(const FrameDev* __restrict__ fp, WaveDev w, uint64_t chunk_start, uint32_t chunk_n) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) w.counters[0] = chunk_n;
+    if (p >= chunk_n) return;
+    const FrameDev& f = *fp;
+    const uint64_t g = chunk_start + p;
+    const uint32_t sample = (uint32_t)(g / f.npix);
+    const uint32_t pix = (uint32_t)(g % f.npix);
+    const uint32_t px = pix % f.width, py = pix / f.width;
+    PathKey pk{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
+    Stream js;
+    js.init(0, KF_RNG_JITTER);
+    const float jx = js.next(pk);
+    const float jy = js.next(pk);
+    const float posx = (float)px + jx, posy = (float)py + jy;
+    const float nx = posx / (float)f.width, ny = posy / (float)f.height;
+    const float dxn = nx * 2.0f - 1.0f, dyn = ny * 2.0f - 1.0f;
+    const float aperture = f.cam.position[3];
+    const float focus = f.cam.front[3];
+    float offx = 0.0f, offy = 0.0f;
+    if (aperture > 0.0f) { // diskSampling (Sampling.glsl:124-134)
+        Stream ls;
+        ls.init(0, KF_RNG_LENS);
+        float qx, qy;
+        do {
+            const float a = ls.next(pk), b = ls.next(pk);
+            qx = 2.0f * a - 1.0f;
+            qy = 2.0f * b - 1.0f;
+        } while (qx * qx + qy * qy >= 1.0f);
+        offx = aperture / 2.0f * qx;
+        offy = aperture / 2.0f * qy;
+    }
+    const float tin[4] = {dxn, dyn, 1.0f, 1.0f};
+    float target[4];
+    mat4_mul(f.cam.proj_inv, tin, target);
+    float origin[4], dir[4];
+    if (aperture > 0.0f) {
+        const float oin[4] = {offx, offy, 0.0f, 1.0f};
+        mat4_mul(f.cam.view_inv, oin, origin);
+        const v3 tv = mk(target[0], target[1], target[2]) * focus - mk(offx, offy, 0.0f);
+        const v3 nd = normalize(tv);
+        const float din[4] = {nd.x, nd.y, nd.z, 0.0f};
+        mat4_mul(f.cam.view_inv, din, dir);
+    } else {
+        const float oin[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+        mat4_mul(f.cam.view_inv, oin, origin);
+        const v3 nd = normalize(mk(target[0], target[1], target[2]));
+        const float din[4] = {nd.x, nd.y, nd.z, 0.0f};
+        mat4_mul(f.cam.view_inv, din, dir);
+    }
+    w.q_o[0][p] = make_float4(origin[0], origin[1], origin[2], __uint_as_float(p));
+    w.q_d[0][p] = make_float4(dir[0], dir[1], dir[2], 0.0f);
+    w.weight[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.radiance[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Closest-hit extension (traceRayEXT with tMin 0.001, tMax 10000).
+// ---------------------------------------------------------------------------
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
+                                                uint32_t depth, uint64_t chunk_start) {
+    const uint32_t count = w.counters[cur];
+    const float4* __restrict__ qo = w.q_o[cur];
+    const float4* __restrict__ qd = w.q_d[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[depth == 0 ? 0 : 1], (unsigned long long)count);
+    TraceCounters cnt{0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float4 o = qo[i], d = qd[i];
+        HitOut h;
+        const uint64_t g = chunk_start + __float_as_uint(o.w);
+        const uint32_t npix = fp->npix;
+        const PathKey pk{make_uint2(fp->seed ^ (uint32_t)(g % npix), fp->camera_index), (uint32_t)(g / npix),
+                         fp->frame};
+        AnyHitCtx ah;
+        ah.pk = &pk;
+        ah.st.init(depth, KF_RNG_ANYHIT);
+        trace<false, COUNT>(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h, cnt, &ah);
+        w.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
+        w.hit_prim[i] = h.prim;
+        if (depth == 0 && w.primary) {
+            const uint32_t p = __float_as_uint(o.w);
+            kf_hit ph;
+            ph.t = h.t; ph.u = h.u; ph.v = h.v; ph.instance = h.inst; ph.prim = h.prim;
+            ph.pad[0] = ph.pad[1] = ph.pad[2] = 0;
+            w.primary[chunk_start + p] = ph;
+        }
+    }
+    if (COUNT) {
+        const uint32_t active = __activemask();
+        if (active == kFull) {
+            warp_add_stat(&w.stats[3], cnt.nodes);
+            warp_add_stat(&w.stats[4], cnt.tris);
+            warp_add_stat(&w.stats[5], cnt.insts);
+        } else {
+            atomicAdd(&w.stats[3], (unsigned long long)cnt.nodes);
+            atomicAdd(&w.stats[4], (unsigned long long)cnt.tris);
+            atomicAdd(&w.stats[5], (unsigned long long)cnt.insts);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shader library (base/Random.glsl, base/Sampling.glsl).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ v3 getPerpendicularVector(v3 u) { // Random.glsl:58-65
+    const v3 a = mk(fabsf(u.x), fabsf(u.y), fabsf(u.z));
+    const uint32_t xm = ((a.x - a.y) < 0.0f && (a.x - a.z) < 0.0f) ? 1u : 0u;
+    const uint32_t ym = (a.y - a.z) < 0.0f ? (1u ^ xm) : 0u;
+    const uint32_t zm = 1u ^ (xm | ym);
+    return cross(u, mk((float)xm, (float)ym, (float)zm));
+}
+__device__ __forceinline__ float Schlick(float cosine, float ior) { // Random.glsl:68-73
+    float r0 = (1.0f - ior) / (1.0f + ior);
+    r0 *= r0;
+    return r0 + (1.0f - r0) * kpow5(1.0f - cosine);
+}
+__device__ __forceinline__ float ggxD(float NdotH, float a2) { // Random.glsl:75-79
+    const float d = fmaxf(NdotH * NdotH * (a2 - 1.0f) + 1.0f, 1e-6f);
+    return a2 / (d * d * KF_REF_PI);
+}
+__device__ __forceinline__ float G1(float d, float a2) { return (2.0f * d) / (d + sqrtf(a2 + (1.0f - a2) * (d * d))); }
+__device__ __forceinline__ float GeometricShadowing(float NdotV, float NdotL, float a2) {
+    return G1(NdotL, a2) * G1(NdotV, a2);
+}
+__device__ __forceinline__ v3 schlickFresnel(v3 f0, float lDotH) { // Random.glsl:133-136
+    const float e = (-5.55473f * lDotH - 6.98316f) * lDotH;
+    return f0 + (splat(1.0f) - f0) * kexp2(e);
+}
+__device__ __forceinline__ v3 sampleGGX(float u0, float u1, float a2, v3 N) { // Random.glsl:83-101
+    const v3 B = getPerpendicularVector(N);
+    const v3 T = cross(B, N);
+    const float cosThetaH = sqrtf(clampf((1.0f - u0) / ((a2 - 1.0f) * u0 + 1.0f), 0.0f, 1.0f));
+    const float sinThetaH = sqrtf(clampf(1.0f - cosThetaH * cosThetaH, 0.0f, 1.0f));
+    const float phiH = u1 * KF_REF_PI * 2.0f;
+    float sp, cp;
+    ksincos(phiH, sp, cp);
+    return T * (sinThetaH * cp) + B * (sinThetaH * sp) + N * cosThetaH;
+}
+__device__ __forceinline__ v3 transformLocalToWorld(v3 dir, v3 n) { // Sampling.glsl:6-23
+    v3 tangent;
+    if (fabsf(n.x) > fabsf(n.y))
+        tangent = mk(n.z, 0.0f, -n.x) / sqrtf(n.x * n.x + n.z * n.z);
+    else
+        tangent = mk(0.0f, -n.z, n.y) / sqrtf(n.y * n.y + n.z * n.z);
+    const v3 bitangent = cross(n, tangent);
+    return dir.x * tangent + dir.y * bitangent + dir.z * n;
+}
+__device__ __forceinline__ v3 cosineHemisphereSampling(float u0, float u1, v3 n) { // Sampling.glsl:25-35
+    const float sq = sqrtf(1.0f - u1);
+    const float ang = 2.0f * KF_REF_PI * u0;
+    float sa, ca;
+    ksincos(ang, sa, ca);
+    return transformLocalToWorld(mk(ca * sq, sa * sq, sqrtf(u1)), n);
+}
+__device__ __forceinline__ v3 uniformSphereSampling(Stream& st, const PathKey& pk) { // Sampling.glsl:72-83
+    v3 p;
+    do {
+        const float a = st.next(pk), b = st.next(pk), c = st.next(pk);
+        p = mk(a, b, c) * 2.0f - splat(1.0f);
+    } while (dot(p, p) >= 1.0f);
+    return p;
+}
+
+// Texture lookup: bilinear, repeat, optional sRGB decode (vkCore.hpp:585,619-637).
+__device__ v3 texture_rgb(const SceneDev& s, int id, float u, float v) {
+    if (id < 0 || (uint32_t)id >= s.num_textures) return splat(1.0f);
+    const uint4 ti = __ldg(s.tex_info + id);
+    const float x = u * (float)ti.y - 0.5f;
+    const float y = v * (float)ti.z - 0.5f;
+    const float fx0 = floorf(x), fy0 = floorf(y);
+    const float ax = x - fx0, ay = y - fy0;
+    const long long ix = (long long)fx0, iy = (long long)fy0;
+    auto wrap = [](long long i, uint32_t n) {
+        long long m = i % (long long)n;
+        return (uint32_t)(m < 0 ? m + n : m);
+    };
+    const uint32_t x0 = wrap(ix, ti.y), x1 = wrap(ix + 1, ti.y);
+    const uint32_t y0 = wrap(iy, ti.z), y1 = wrap(iy + 1, ti.z);
+    const uchar4 t00 = __ldg(s.texels + ti.x + (size_t)y0 * ti.y + x0);
+    const uchar4 t10 = __ldg(s.texels + ti.x + (size_t)y0 * ti.y + x1);
+    const uchar4 t01 = __ldg(s.texels + ti.x + (size_t)y1 * ti.y + x0);
+    const uchar4 t11 = __ldg(s.texels + ti.x + (size_t)y1 * ti.y + x1);
+    auto dec = [&](unsigned char b) { return ti.w ? __ldg(s.srgb_decode + b) : (float)b / 255.0f; };
+    float out[3];
+    const unsigned char c00[3] = {t00.x, t00.y, t00.z}, c10[3] = {t10.x, t10.y, t10.z};
+    const unsigned char c01[3] = {t01.x, t01.y, t01.z}, c11[3] = {t11.x, t11.y, t11.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float top = dec(c00[c]) * (1.0f - ax) + dec(c10[c]) * ax;
+        const float bot = dec(c01[c]) * (1.0f - ax) + dec(c11[c]) * ax;
+        out[c] = top * (1.0f - ay) + bot * ay;
+    }
+    return mk(out[0], out[1], out[2]);
+}
+
+struct Shading {
+    float f, a2;
+    v3 diffuseColor, specularColor, transmissionColor;
+    bool isInside;
+};
+
+// calcDirectContribution (PathTrace.rchit:103-171).
+__device__ v3 calcDirectContribution(Stream& st, const PathKey& pk, v3 L, v3 V, v3 N, v3 lightEmission,
+                                     const Shading& sh) {
+    v3 weight = splat(0.0f);
+    const float a2 = sh.a2, f = sh.f;
+    if (sh.transmissionColor != splat(0.0f)) {
+        if (sh.isInside) {
+            weight = splat(0.0f);
+        } else {
+            const float NdotV0 = dot(N, V);
+            const v3 refractedL = refract(-V, N, 1.0f / f);
+            const float reflectProb = refractedL != splat(0.0f) ? Schlick(NdotV0, f) : 1.0f;
+            if (st.next(pk) <= reflectProb) {
+                const v3 H = normalize(L + V);
+                const float NdotL = dot(N, L);
+                const float NdotH = dot(N, H);
+                const float HdotV = dot(H, V);
+                const float NdotV = fmaxf(dot(N, V), 1e-6f);
+                const float LdotH = dot(L, H);
+                const float D = ggxD(NdotH, a2);
+                const float G = GeometricShadowing(NdotL, NdotV, a2);
+                const v3 F = schlickFresnel(sh.transmissionColor, LdotH);
+                weight = D * F * G * HdotV / NdotH * NdotV;
+            } else {
+                weight = splat(0.0f);
+            }
+        }
+    } else {
+        const v3 H = normalize(L + V);
+        const float NdotL = dot(N, L);
+        const float NdotH = dot(N, H);
+        const float HdotV = dot(H, V);
+        const float NdotV = fmaxf(dot(N, V), 1e-6f);
+        const float LdotH = dot(L, H);
+        const float D = ggxD(NdotH, a2);
+        const float G = GeometricShadowing(NdotL, NdotV, a2);
+        const v3 F = schlickFresnel(sh.specularColor, LdotH);
+        const float diffuseLum = length(sh.diffuseColor);
+        const float specularLum = length(sh.specularColor);
+        float probDiffuse = diffuseLum / (diffuseLum + specularLum);
+        if (diffuseLum == 0.0f && specularLum == 0.0f) probDiffuse = 0.5f;
+        const v3 diffuseWeight = sh.diffuseColor * splat(NdotL);
+        const v3 specularWeight = D * F * G * HdotV / NdotH * NdotV;
+        weight = st.next(pk) < probDiffuse ? diffuseWeight * probDiffuse : specularWeight * (1.0f - probDiffuse);
+    }
+    return lightEmission * weight;
+}
+
+// One light slot's sample: returns true if a shadow ray is needed (NdotL > 0 and a
+// non-zero contribution), with its direction, length and contribution.
+__device__ bool light_sample(const SceneDev& s, uint32_t slot, uint32_t depth, const PathKey& pk, v3 worldPos, v3 N,
+                             v3 V, const Shading& sh, v3& Lout, float& tmax, v3& contrib) {
+    const uint32_t group = s.slot_group[slot], li = s.slot_index[slot];
+    Stream st;
+    v3 L, lightEmission;
+    float maxDist;
+    if (group == 0) { // traceDirectionalLight (rchit:204-223)
+        const kf_dir_light_ubo* dl = s.dlight;
+        st.init(depth, KF_RNG_DIRLIGHT);
+        lightEmission = ld3(dl->rgbs) * dl->rgbs[3];
+        if (lightEmission == splat(0.0f)) return false;
+        L = -ld3(dl->direction);
+        if (dl->direction[3] != 0.0f) {
+            const float a = st.next(pk), b = st.next(pk), c = st.next(pk);
+            L = normalize(L + dl->direction[3] * mk(a, b, c));
+        }
+        maxDist = KF_DIR_LIGHT_TMAX;
+    } else if (group == 1) { // tracePointLights (rchit:227-258)
+        const kf_point_lights_ubo* pl = s.plights;
+        st.init(depth, KF_RNG_POINT0 + li);
+        if (!(pl->rgbs[li][3] > 0.0f)) return false;
+        const float lum = length(ld3(pl->rgbs[li]) * pl->rgbs[li][3]);
+        if (lum == 0.0f) return false;
+        v3 lpos = ld3(pl->posr[li]);
+        if (pl->posr[li][3] != 0.0f) {
+            const v3 perturb = uniformSphereSampling(st, pk);
+            lpos = lpos + pl->posr[li][3] * normalize(perturb);
+        }
+        L = lpos - worldPos;
+        const float d = length(L);
+        L = normalize(L);
+        lightEmission = ld3(pl->rgbs[li]) * pl->rgbs[li][3] / d / d;
+        maxDist = d;
+    } else { // traceActiveLights (rchit:262-316)
+        const kf_active_lights_ubo* al = s.alights;
+        st.init(depth, KF_RNG_ACTIVE0 + li);
+        if (!(al->front[li][3] > 0.0f)) return false;
+        const float lum = length(ld3(al->rgbs[li]) * al->rgbs[li][3]);
+        if (lum == 0.0f) return false;
+        const float softness = al->sftp[li][0];
+        v3 lpos = ld3(al->position[li]);
+        if (softness != 0.0f) {
+            const v3 perturb = uniformSphereSampling(st, pk);
+            lpos = lpos + softness * normalize(perturb);
+        }
+        L = lpos - worldPos;
+        const float d = length(L);
+        L = normalize(L);
+        const float fov = al->sftp[li][1];
+        const v3 alightDir = normalize(ld3(al->front[li]));
+        const float halfAngle = clampf(fov, 0.0f, KF_REF_PI) / 2.0f;
+        const float cos_ = dot(alightDir, -L);
+        if (!(cos_ > kcos(halfAngle))) return false;
+        const int texID = (int)al->sftp[li][2];
+        v3 color = ld3(al->rgbs[li]);
+        if (texID >= 0) {
+            // proj * view * vec4(worldPos, 1) = (proj * view) * vec4(...)
+            const float* P = al->proj[li];
+            const float* Vw = al->view[li];
+            float pv[16];
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    pv[c * 4 + r] = P[0 * 4 + r] * Vw[c * 4 + 0] + P[1 * 4 + r] * Vw[c * 4 + 1] +
+                                    P[2 * 4 + r] * Vw[c * 4 + 2] + P[3 * 4 + r] * Vw[c * 4 + 3];
+            const float wp[4] = {worldPos.x, worldPos.y, worldPos.z, 1.0f};
+            float tc[4];
+            mat4_mul(pv, wp, tc);
+            const float ww = tc[3];
+            for (int k = 0; k < 4; ++k) tc[k] = tc[k] / ww;
+            color = color * texture_rgb(s, texID, tc[0] * 0.5f + 0.5f, tc[1] * 0.5f + 0.5f);
+        }
+        lightEmission = color * al->rgbs[li][3] / d / d;
+        maxDist = d;
+    }
+    // traceShadowRay (rchit:175-200): only NdotL > 0 traces; the lobe draw is the
+    // next draw of this light's stream.
+    if (!(dot(N, L) > 0.0f)) return false;
+    contrib = calcDirectContribution(st, pk, L, V, N, lightEmission, sh);
+    if (contrib == splat(0.0f)) return false;
+    Lout = L;
+    tmax = maxDist;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Shade: miss / emission / PrincipledBSDF (rchit:322-468), light samples, RR.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
+                                               uint32_t depth, uint64_t chunk_start) {
+    const FrameDev& f = *fp;
+    const uint32_t count = w.counters[cur];
+    const int nxt = cur ^ 1;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count; base += stride) {
+        const uint32_t i = base + lane;
+        const bool valid = i < count;
+        uint32_t p = 0;
+        uint64_t g = 0;
+        PathKey pk;
+        bool is_mat = false, cont = false;
+        v3 worldPos = splat(0.0f), N = splat(0.0f), V = splat(0.0f), L = splat(0.0f);
+        v3 wnew = splat(0.0f), wcont = splat(0.0f);
+        Shading sh;
+        sh.f = 1.0f; sh.a2 = 0.0f;
+        sh.diffuseColor = sh.specularColor = sh.transmissionColor = splat(0.0f);
+        sh.isInside = false;
+        if (valid) {
+            const float4 qo = w.q_o[cur][i], qd = w.q_d[cur][i];
+            p = __float_as_uint(qo.w);
+            g = chunk_start + p;
+            const uint32_t sample = (uint32_t)(g / f.npix);
+            const uint32_t pix = (uint32_t)(g % f.npix);
+            pk = PathKey{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
+            const float4 hv = w.hit[i];
+            const uint32_t inst = __float_as_uint(hv.w);
+            const float4 w4 = w.weight[p];
+            const v3 wold = mk(w4.x, w4.y, w4.z);
+            float4 col4 = w.radiance[g];
+            v3 color = mk(col4.x, col4.y, col4.z);
+            const v3 rayD = mk(qd.x, qd.y, qd.z);
+            if (inst == kMiss) {
+                // PathTrace.rmiss:12-31 (clear colour; environment cube maps are not provided)
+                const v3 emission = ld3(f.pc.clear_color) * f.pc.clear_color[3];
+                color = color + emission * wold;
+                w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
+            } else {
+                const uint32_t prim = w.hit_prim[i];
+                const InstanceRec* ip = s.inst + inst;
+                const float4 m0 = __ldg(&ip->w2o0), m1 = __ldg(&ip->w2o1), m2 = __ldg(&ip->w2o2);
+                const uint32_t geom = __ldg(&ip->geometry);
+                const uint4 gi = __ldg(s.geom + geom);
+                const uint32_t tri = gi.y + prim;
+                const uint32_t i0 = __ldg(s.indices + 3 * (size_t)tri + 0) + gi.x;
+                const uint32_t i1 = __ldg(s.indices + 3 * (size_t)tri + 1) + gi.x;
+                const uint32_t i2 = __ldg(s.indices + 3 * (size_t)tri + 2) + gi.x;
+                const float4 a0 = __ldg(s.verts + 3 * (size_t)i0), a1 = __ldg(s.verts + 3 * (size_t)i0 + 1),
+                             a2v = __ldg(s.verts + 3 * (size_t)i0 + 2);
+                const float4 b0 = __ldg(s.verts + 3 * (size_t)i1), b1 = __ldg(s.verts + 3 * (size_t)i1 + 1),
+                             b2 = __ldg(s.verts + 3 * (size_t)i1 + 2);
+                const float4 c0 = __ldg(s.verts + 3 * (size_t)i2), c1 = __ldg(s.verts + 3 * (size_t)i2 + 1),
+                             c2 = __ldg(s.verts + 3 * (size_t)i2 + 2);
+                const kf_material_gpu mat = s.materials[__ldg(s.matidx + tri)];
+                const v3 emission = ld3(mat.emission) * mat.emission[3];
+                if (emission != splat(0.0f)) {
+                    // emissive hit ends the path (rchit:330-335)
+                    color = color + (ld3(mat.emission) * mat.emission[3]) * wold;
+                    w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
+                } else {
+                    // getShadingData (rchit:66-98); unpackVertex: pos = d0.xyz,
+                    // normal = (d0.w, d1.x, d1.y), uv = (d2.y, d2.z)
+                    const float bx = 1.0f - hv.y - hv.z, by = hv.y, bz = hv.z;
+                    const v3 n0 = mk(a0.w, a1.x, a1.y), n1 = mk(b0.w, b1.x, b1.y), n2 = mk(c0.w, c1.x, c1.y);
+                    const v3 ln = n0 * bx + n1 * by + n2 * bz;
+                    const v3 wn = mk(ln.x * m0.x + ln.y * m1.x + ln.z * m2.x, ln.x * m0.y + ln.y * m1.y + ln.z * m2.y,
+                                     ln.x * m0.z + ln.y * m1.z + ln.z * m2.z);
+                    N = normalize(wn);
+                    const v3 rayO = mk(qo.x, qo.y, qo.z);
+                    worldPos = rayO + rayD * hv.x;
+                    const float uvx = a2v.y * bx + b2.y * by + c2.y * bz;
+                    const float uvy = a2v.z * bx + b2.z * by + c2.z * bz;
+                    // facing in object space: front when dir opposes (v1-v0)x(v2-v0)
+                    bool backface;
+                    {
+                        const float odx = m0.x * rayD.x + m0.y * rayD.y + m0.z * rayD.z;
+                        const float ody = m1.x * rayD.x + m1.y * rayD.y + m1.z * rayD.z;
+                        const float odz = m2.x * rayD.x + m2.y * rayD.y + m2.z * rayD.z;
+                        const v3 e1 = mk(b0.x, b0.y, b0.z) - mk(a0.x, a0.y, a0.z);
+                        const v3 e2 = mk(c0.x, c0.y, c0.z) - mk(a0.x, a0.y, a0.z);
+                        backface = dot(mk(odx, ody, odz), cross(e1, e2)) > 0.0f;
+                    }
+                    v3 baseColor = ld3(mat.diffuse);
+                    if (mat.diffuse_tex >= 0) baseColor = texture_rgb(s, mat.diffuse_tex, uvx, uvy);
+                    baseColor = baseColor / KF_REF_PI;
+                    const float metallic =
+                        mat.metallic_tex >= 0 ? texture_rgb(s, mat.metallic_tex, uvx, uvy).x : mat.metallic;
+                    const float roughness =
+                        mat.roughness_tex >= 0 ? texture_rgb(s, mat.roughness_tex, uvx, uvy).x : mat.roughness;
+                    const float a2 = roughness * roughness;
+                    const float transmission = mat.transmission_tex >= 0
+                                                   ? texture_rgb(s, mat.transmission_tex, uvx, uvy).x
+                                                   : mat.transmission;
+                    const float fi = fmaxf(mat.ior, 1e-5f);
+                    const float diffuse_weight =
+                        (1.0f - clampf(metallic, 0.0f, 1.0f)) * (1.0f - clampf(transmission, 0.0f, 1.0f));
+                    const float final_transmission =
+                        clampf(transmission, 0.0f, 1.0f) * (1.0f - clampf(metallic, 0.0f, 1.0f));
+                    const float specular_weight = (1.0f - final_transmission);
+                    v3 weight = splat(0.0f);
+                    V = normalize(-rayD);
+                    const bool isInside = backface;
+                    N = isInside ? -N : N;
+                    L = splat(0.0f);
+                    const float NdotV = dot(N, V);
+                    const v3 diffuseColor = diffuse_weight * baseColor;
+                    const v3 specularColor =
+                        specular_weight * (baseColor * metallic + (mat.specular * 0.08f * splat(1.0f)) * (1.0f - metallic));
+                    const v3 transmissionColor = transmission * baseColor;
+                    const float diffuseLum = length(diffuseColor);
+                    const float specularLum = length(specularColor);
+                    float probDiffuse = diffuseLum / (diffuseLum + specularLum);
+                    if (diffuseLum == 0.0f && specularLum == 0.0f) {
+                        if (baseColor == splat(0.0f)) {
+                            if (diffuse_weight == 1.0f) probDiffuse = 1.0f;
+                            else if (diffuse_weight == 0.0f) probDiffuse = 0.0f;
+                            else probDiffuse = 0.5f;
+                        } else
+                            probDiffuse = 0.0f;
+                    } else {
+                        probDiffuse *= specular_weight;
+                    }
+                    Stream bs;
+                    bs.init(depth, KF_RNG_BSDF);
+                    const bool chooseDiffuse = bs.next(pk) < probDiffuse;
+                    if (chooseDiffuse) {
+                        const float u0 = bs.next(pk), u1 = bs.next(pk);
+                        L = cosineHemisphereSampling(u0, u1, N);
+                        const float NdotL = clampf(dot(N, L), 0.0f, 1.0f);
+                        weight = KF_REF_PI * diffuseColor * NdotL / probDiffuse;
+                    }
+                    if (!chooseDiffuse) {
+                        if (final_transmission == 0.0f) {
+                            const float u0 = bs.next(pk), u1 = bs.next(pk);
+                            const v3 H = sampleGGX(u0, u1, a2, N);
+                            const float HdotV = dot(H, V);
+                            L = 2.0f * HdotV * H - V;
+                            const float NoV = fmaxf(dot(N, V), 1e-7f);
+                            const float NoL = dot(N, L);
+                            const float NoH = fmaxf(dot(N, H), 1e-7f);
+                            const float VoH = fmaxf(dot(V, H), 1e-7f);
+                            if (NoL >= 0.0f) {
+                                const float G = GeometricShadowing(NoV, NoL, a2);
+                                const v3 F = schlickFresnel(specularColor, VoH);
+                                weight = KF_REF_PI * F * G * VoH / (NoH * NoV * (1.0f - probDiffuse));
+                            } else
+                                weight = splat(0.0f);
+                        } else {
+                            const float ior = isInside ? 1.0f / fi : fi;
+                            const float _dot = isInside ? NdotV * ior : NdotV;
+                            const v3 refractedL = refract(-V, N, 1.0f / fi);
+                            const float reflectProb = refractedL != splat(0.0f) ? Schlick(_dot, fi) : 1.0f;
+                            if (bs.next(pk) >= reflectProb) {
+                                L = refractedL;
+                                weight = KF_REF_PI * transmissionColor / (1.0f - probDiffuse);
+                            } else {
+                                L = reflect(-V, N);
+                                weight = KF_REF_PI * transmissionColor / (1.0f - probDiffuse);
+                            }
+                        }
+                    }
+                    sh.f = fi;
+                    sh.a2 = a2;
+                    sh.diffuseColor = diffuseColor;
+                    sh.specularColor = specularColor;
+                    sh.transmissionColor = transmissionColor;
+                    sh.isInside = isInside;
+                    // AOVs of sample 0, first bounce (rgen:114-117)
+                    if (depth == 0 && sample == 0) {
+                        w.albedo[pix] = make_float4(baseColor.x, baseColor.y, baseColor.z, 1.0f);
+                        w.normal[pix] = make_float4(N.x, N.y, N.z, 1.0f);
+                    }
+                    // rgen:110  weight *= ray.weight
+                    wnew = wold * weight;
+                    if (wnew != splat(0.0f)) {
+                        is_mat = true;
+                        bool alive = true;
+                        wcont = wnew;
+                        if (f.pc.russian_roulette && depth >= f.pc.rr_min_bounces) { // rgen:124-138
+                            const float pr = fmaxf(wnew.x, fmaxf(wnew.y, wnew.z));
+                            Stream rs;
+                            rs.init(depth, KF_RNG_RR);
+                            const float rnd = rs.next(pk);
+                            if (rnd > pr)
+                                alive = false;
+                            else
+                                wcont = wnew * (1.0f / pr);
+                        }
+                        cont = alive && (depth + 1 <= f.pc.max_path_depth);
+                    }
+                }
+            }
+            if (depth == 0 && sample == 0) w.depth[pix] = inst == kMiss ? 0.0f : hv.x;
+        }
+        // light slots: one warp-uniform loop, one ballot per slot
+        uint64_t req = 0;
+        for (uint32_t j = 0; j < s.num_slots; ++j) {
+            v3 Ls = splat(0.0f), c = splat(0.0f);
+            float tmax = 0.0f;
+            const bool emit = is_mat && light_sample(s, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
+            const uint32_t pos = warp_append(emit, &w.counters[2]);
+            if (emit) {
+                w.sq_o[pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
+                w.sq_d[pos] = make_float4(Ls.x, Ls.y, Ls.z, __uint_as_float((j << 26) | p));
+                w.contrib[(size_t)j * w.chunk_cap + p] = make_float4(c.x, c.y, c.z, 0.0f);
+                w.vis[(size_t)j * w.chunk_cap + p] = 0;
+                req |= 1ull << j;
+            }
+        }
+        if (valid) {
+            w.req[p] = req;
+            if (req) w.nee_w[p] = make_float4(wnew.x, wnew.y, wnew.z, 0.0f);
+        }
+        const uint32_t pos = warp_append(cont, &w.counters[nxt]);
+        if (cont) {
+            w.q_o[nxt][pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, __uint_as_float(p));
+            w.q_d[nxt][pos] = make_float4(L.x, L.y, L.z, 0.0f);
+            w.weight[p] = make_float4(wcont.x, wcont.y, wcont.z, 0.0f);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shadow rays: any hit in [0.001, tmax] (rchit:175-200, PathTraceShadow.rmiss).
+// ---------------------------------------------------------------------------
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_shadow(SceneDev s, WaveDev w) {
+    const uint32_t count = w.counters[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[2], (unsigned long long)count);
+    TraceCounters cnt{0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float4 o = w.sq_o[i], d = w.sq_d[i];
+        HitOut h;
+        const bool occluded = trace<true, COUNT>(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w, h, cnt);
+        if (!occluded) {
+            const uint32_t tag = __float_as_uint(d.w);
+            const uint32_t slot = tag >> 26, p = tag & ((1u << 26) - 1u);
+            w.vis[(size_t)slot * w.chunk_cap + p] = 1;
+        }
+    }
+    if (COUNT) {
+        atomicAdd(&w.stats[6], (unsigned long long)cnt.nodes);
+        atomicAdd(&w.stats[7], (unsigned long long)cnt.tris);
+        atomicAdd(&w.stats[8], (unsigned long long)cnt.insts);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gather: shadow_color = traceDirectionalLight + tracePointLights + traceActiveLights
+// (rchit:457-460), color += shadow_color * weight (rgen:111).
+// ---------------------------------------------------------------------------
+__global__ void k_gather(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur, uint64_t chunk_start) {
+    const uint32_t count = w.counters[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t p = __float_as_uint(w.q_o[cur][i].w);
+        uint64_t req = w.req[p];
+        if (!req) continue;
+        v3 D = splat(0.0f), P = splat(0.0f), A = splat(0.0f);
+        while (req) {
+            const uint32_t j = __ffsll((long long)req) - 1;
+            req &= req - 1;
+            if (!w.vis[(size_t)j * w.chunk_cap + p]) continue;
+            const float4 c4 = w.contrib[(size_t)j * w.chunk_cap + p];
+            const v3 c = mk(c4.x, c4.y, c4.z);
+            const uint32_t grp = s.slot_group[j];
+            if (grp == 0) D = c;
+            else if (grp == 1) P = P + c;
+            else A = A + c;
+        }
+        const v3 shadow = (D + P) + A;
+        const float4 wn = w.nee_w[p];
+        const uint64_t g = chunk_start + p;
+        const float4 col = w.radiance[g];
+        const v3 color = mk(col.x, col.y, col.z) + shadow * mk(wn.x, wn.y, wn.z);
+        w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-pixel resolve: finalColor = colors / spp (rgen:140-144) and the running
+// mean over frames (rgen:151-163); FP64 sum of finalColor alongside.
+// ---------------------------------------------------------------------------
+__global__ void k_resolve(const FrameDev* __restrict__ fp, const float4* __restrict__ radiance, uint32_t npix,
+                          uint32_t spp, float4* accum, dbl4* sum64) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    const int32_t frame_count = fp->pc.frame_count;
+    v3 colors = splat(0.0f);
+    for (uint32_t sidx = 0; sidx < spp; ++sidx) {
+        const float4 c = radiance[(size_t)sidx * npix + pix];
+        colors = colors + mk(c.x, c.y, c.z);
+    }
+    const v3 fin = colors / (float)spp;
+    if (frame_count <= 0) {
+        accum[pix] = make_float4(fin.x, fin.y, fin.z, 1.0f);
+        sum64[pix] = make_dbl4(fin.x, fin.y, fin.z, 1.0);
+    } else {
+        const float4 old = accum[pix];
+        const float a = 1.0f / (float)(frame_count + 1);
+        // mix(x, y, a) = x * (1 - a) + y * a
+        accum[pix] = make_float4(old.x * (1.0f - a) + fin.x * a, old.y * (1.0f - a) + fin.y * a,
+                                 old.z * (1.0f - a) + fin.z * a, 1.0f);
+        const dbl4 s = sum64[pix];
+        sum64[pix] = make_dbl4(s.x + fin.x, s.y + fin.y, s.z + fin.z, s.w + 1.0);
+    }
+}
+
+__constant__ float c_srgb_thresh[256];
+
+__device__ __forceinline__ unsigned char srgb8(float v) {
+    if (!(v > 0.0f)) return 0;
+    int lo = 0;
+#pragma unroll
+    for (int step = 128; step >= 1; step >>= 1)
+        if (c_srgb_thresh[lo + step] <= v) lo += step;
+    return (unsigned char)lo;
+}
+
+// Linear RGBA32F -> B8G8R8A8 sRGB (config.hpp:144, PostProcessing.frag:11-17).
+__global__ void k_srgb(const float4* __restrict__ img, uint32_t npix, uchar4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    const float4 c = img[i];
+    out[i] = make_uchar4(srgb8(c.z), srgb8(c.y), srgb8(c.x), 255);
+}
+
+// FP64 relative MSE: sum over rgb of (x - r)^2 / (r^2 + eps), per-block partials then one final block.
+__global__ void k_relmse_partial(const float4* __restrict__ x, const float4* __restrict__ ref, uint64_t n, double eps,
+                                 double* partial) {
+    double acc = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 a = x[i], b = ref[i];
+        const double d0 = (double)a.x - b.x, d1 = (double)a.y - b.y, d2 = (double)a.z - b.z;
+        acc += d0 * d0 / ((double)b.x * b.x + eps) + d1 * d1 / ((double)b.y * b.y + eps) +
+               d2 * d2 / ((double)b.z * b.z + eps);
+    }
+    __shared__ double sm[256];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off; off >>= 1) {
+        if ((int)threadIdx.x < off) sm[threadIdx.x] += sm[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+__global__ void k_relmse_final(const double* partial, uint32_t blocks, uint64_t n, double* out) {
+    __shared__ double sm[256];
+    double acc = 0.0;
+    for (uint32_t i = threadIdx.x; i < blocks; i += blockDim.x) acc += partial[i];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off; off >>= 1) {
+        if ((int)threadIdx.x < off) sm[threadIdx.x] += sm[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0] / (3.0 * (double)n);
+}
+
+} // namespace
+
+void launch_raygen(const FrameDev* f, const WaveDev& w, uint64_t chunk_start, uint32_t chunk_n, cudaStream_t st) {
+    k_raygen<<<(chunk_n + 255) / 256, 256, 0, st>>>(f, w, chunk_start, chunk_n);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_extend(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
+                   uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st) {
+    if (count_mode)
+        k_extend<true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+    else
+        k_extend<false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_shade(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
+                  uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
+    k_shade<<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_shadow(const SceneDev& s, const WaveDev& w, uint32_t grid, bool count_mode, cudaStream_t st) {
+    if (count_mode)
+        k_shadow<true><<<grid, 128, 0, st>>>(s, w);
+    else
+        k_shadow<false><<<grid, 128, 0, st>>>(s, w);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_gather(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint64_t chunk_start,
+                   uint32_t grid, cudaStream_t st) {
+    k_gather<<<grid, 256, 0, st>>>(s, f, w, cur, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_resolve(const FrameDev* f, const float4* radiance, uint32_t npix, uint32_t spp, float4* accum,
+                    dbl4* sum64, cudaStream_t st) {
+    k_resolve<<<(npix + 255) / 256, 256, 0, st>>>(f, radiance, npix, spp, accum, sum64);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_srgb(const float4* img, uint32_t npix, uchar4* out, cudaStream_t st) {
+    k_srgb<<<(npix + 255) / 256, 256, 0, st>>>(img, npix, out);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void upload_srgb_thresholds(const float* thresh256) {
+    KF_CUDA_CHECK(cudaMemcpyToSymbol(c_srgb_thresh, thresh256, sizeof(float) * 256));
+}
+void launch_relmse(const float4* x, const float4* ref, uint64_t n, double eps, double* partial, uint32_t blocks,
+                   double* out, cudaStream_t st) {
+    k_relmse_partial<<<blocks, 256, 0, st>>>(x, ref, n, eps, partial);
+    k_relmse_final<<<1, 256, 0, st>>>(partial, blocks, n, out);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+
+} // namespace kf
