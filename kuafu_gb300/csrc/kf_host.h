@@ -87,6 +87,7 @@ struct SceneGpu {
     uint64_t built_material_version = 0;
     uint64_t built_texture_version = 0;
     uint32_t blas_node_count = 0, tlas_node_count = 0;
+    uint64_t generation = 0; // bumped whenever a device buffer may have moved
     kf::SceneDev view{};
 };
 

@@ -329,10 +329,10 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
         // The launch sequence depends only on buffer addresses and sizes; the
         // per-frame values live in frame_dev, so a captured graph replays as is.
         char key[512];
-        std::snprintf(key, sizeof(key), "%p|%p|%p|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u", (void*)s, (void*)c,
-                      (void*)sv.blas_nodes, npix, spp, r->cfg.path_depth, (unsigned long long)npaths, chunk,
-                      (void*)w.q_o[0], (void*)w.radiance, (void*)w.contrib, (void*)sv.tlas_nodes, (void*)sv.materials,
-                      sv.num_slots, 0u);
+        std::snprintf(key, sizeof(key), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u", (void*)s, (void*)c,
+                      (unsigned long long)s->gpu.generation, npix, spp, r->cfg.path_depth,
+                      (unsigned long long)npaths, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)w.contrib,
+                      (void*)c->accum.ptr, (void*)w.primary, sv.num_slots, r->cfg.russian_roulette);
         if (!r->graph_exec || r->graph_key != key) {
             if (r->graph_exec) {
                 cudaGraphExecDestroy(r->graph_exec);

@@ -250,9 +250,17 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
     }
     if (G.built_material_version != g_material_version || rebuilt_geom) {
         std::vector<kf_material_gpu> mats = flatten_materials();
+        // every triangle must name an existing material: the kernels index the table unchecked
+        for (const kf_geometry_s* g : s->geometries) {
+            const size_t ntri = g->indices.size() / 3;
+            for (size_t t = 0; t < ntri; ++t)
+                KF_REQUIRE(g->mat_index[t] < mats.size(), KF_ERR_OUT_OF_RANGE,
+                           "a geometry's matIndex names a material that does not exist");
+        }
         if (mats.empty()) mats.push_back(kf_material_gpu{});
         G.materials.upload(mats.data(), mats.size(), st);
         G.built_material_version = g_material_version;
+        ++G.generation;
     }
     if (G.built_texture_version != g_texture_version || G.srgb_decode.count == 0) {
         std::vector<uint4> info;
@@ -269,6 +277,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         const std::vector<float>& dec = srgb_decode_table();
         G.srgb_decode.upload(dec.data(), dec.size(), st);
         G.built_texture_version = g_texture_version;
+        ++G.generation;
     }
     if (rebuilt_geom || G.built_inst_stamp != s->inst_stamp) {
         built_any = true;
@@ -338,6 +347,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         }
         G.built_inst_stamp = s->inst_stamp;
     }
+    if (built_any || rebuilt_geom) ++G.generation;
     if (timing) {
         KF_CUDA_CHECK(cudaEventRecord(e1, st));
         KF_CUDA_CHECK(cudaEventSynchronize(e1));

