@@ -229,6 +229,12 @@ def run_ours(args):
         rays_all = float(rays)
     value = rays_all / (t_ms / 1e3) / 1e6
     rays_per_frame = rays / args.steps
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "quick": True,
+                              "ms_per_step": t_ms / args.steps, "config": dict(WORKLOAD), "clocks": clk}), flush=True)
+        r.close()
+        return 0
 
     # e2e: the public API with host buffers: run + download of the BGRA frame per step
     host = torch.empty((WORKLOAD["height"], WORKLOAD["width"], 4), dtype=torch.uint8).pin_memory()
@@ -316,9 +322,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--width", type=int, default=None, help="profiling: smaller frame of the same scene")
+    ap.add_argument("--height", type=int, default=None)
+    ap.add_argument("--quick", action="store_true",
+                    help="profiling: timed steps only (no e2e, counting or CPU-baseline passes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.width:
+        WORKLOAD["width"] = args.width
+    if args.height:
+        WORKLOAD["height"] = args.height
     from kuafu_gb300 import build
 
     build.build_oracle()

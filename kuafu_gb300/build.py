@@ -93,6 +93,21 @@ def build_libkf(verbose: bool = False, ptxas: bool = False, force: bool = False)
     return LIB
 
 
+EXAMPLE_SRC = ROOT / "examples" / "cornell_facade.cpp"
+EXAMPLE_BIN = BUILD / "cornell_facade"
+
+
+def build_example(verbose: bool = False, force: bool = False) -> Path:
+    """The C++ facade example (include/kuafu_gb300/kuafu.hpp over libkf)."""
+    BUILD.mkdir(exist_ok=True)
+    deps = [EXAMPLE_SRC, ROOT / "include" / "kuafu_gb300" / "kuafu.hpp", ROOT / "include" / "kf.h", LIB]
+    if force or _stale(EXAMPLE_BIN, deps):
+        cxx = os.environ.get("CXX", "g++")
+        _run([cxx, "-std=c++17", "-O2", "-I", str(ROOT / "include"), "-o", str(EXAMPLE_BIN), str(EXAMPLE_SRC),
+              "-L", str(PKG), "-lkf", f"-Wl,-rpath,{PKG}"], verbose)
+    return EXAMPLE_BIN
+
+
 def build_oracle(verbose: bool = False, force: bool = False) -> Path:
     src = ORACLE_DIR / "kf_oracle.cpp"
     deps = [src, ORACLE_DIR / "kf_oracle.h", ROOT / "include" / "kf_types.h"]
@@ -111,7 +126,8 @@ def main(argv=None) -> int:
     a = ap.parse_args(argv)
     build_oracle(a.verbose, a.force)
     build_libkf(a.verbose, a.ptxas, a.force)
-    print(f"built {LIB} and {ORACLE_LIB}")
+    build_example(a.verbose, a.force)
+    print(f"built {LIB}, {ORACLE_LIB} and {EXAMPLE_BIN}")
     return 0
 
 
