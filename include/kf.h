@@ -252,6 +252,20 @@ KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint
 KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
                      double* out);
 
+/* The same reduction for callers that cannot call cudaMalloc: an application
+ * whose device memory is owned by its own pool allocator, or a frame loop that
+ * must not take the device-wide synchronisation cudaMalloc / cudaFree imply.
+ * It allocates nothing: its per-block partials live in a static device array of
+ * 4096 + 1 doubles (32 KiB) that every GPU loading libkf keeps until exit.
+ * Limit: num_pixels <= 268435456 (4096 blocks x 65536 pixels), else KF_ERR_LIMIT.
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) of the current device;
+ * the first call on a device looks up the array's device address, so make that
+ * first call before any stream capture. Calls share the array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised by the
+ * caller. Blocks until *out is written. No counterpart in the reference. */
+KF_API int kf_relmse_noalloc(const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
+                             void* stream, double* out);
+
 #ifdef __cplusplus
 }
 #endif

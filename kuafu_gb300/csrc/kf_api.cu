@@ -50,7 +50,13 @@ using namespace kf;
 
 namespace {
 thread_local std::string t_error;
+}
 
+namespace kf {
+void set_last_error(const std::string& msg) { t_error = msg; }
+}
+
+namespace {
 int fail(int code, const std::string& msg) {
     t_error = msg;
     return code;

@@ -16,6 +16,9 @@
 // written, matching the CPU oracle operation for operation.
 #include "kf_wavefront.h"
 
+#include <mutex>
+#include <string>
+
 #include "kf_util.h"
 
 namespace kf {
@@ -941,3 +944,76 @@ void launch_relmse(const float4* x, const float4* ref, uint64_t n, double eps, d
 }
 
 } // namespace kf
+
+// ---------------------------------------------------------------------------
+// kf_relmse_noalloc: the relative-MSE reduction for callers that cannot call
+// cudaMalloc (an embedding application whose device memory belongs to its own
+// pool allocator, or a frame loop that must not take the implicit device-wide
+// synchronisation of cudaMalloc / cudaFree). The per-block FP64 partials live
+// in this file-scope device array instead of allocated scratch. Every GPU that
+// loads the library holds it (32 KiB + 8 B) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint32_t kNoAllocMaxBlocks = 4096;
+constexpr uint64_t kNoAllocPixelsPerBlock = 65536;
+static __device__ __align__(256) double g_relmse_scratch[kNoAllocMaxBlocks + 1];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {}; // device address of g_relmse_scratch, per device ordinal
+} // namespace
+
+namespace kf {
+void set_last_error(const std::string& msg);
+}
+
+extern "C" KF_API int kf_relmse_noalloc(const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
+                                        void* stream, double* out) {
+    if (!x_dev || !ref_dev || !out || num_pixels == 0) {
+        kf::set_last_error("kf_relmse_noalloc: null pointer or zero pixels");
+        return KF_ERR_INVALID_ARGUMENT;
+    }
+    if (num_pixels > (uint64_t)kNoAllocMaxBlocks * kNoAllocPixelsPerBlock) {
+        kf::set_last_error("kf_relmse_noalloc: more than 268435456 pixels (4096 blocks x 65536 pixels) do not fit "
+                           "its static scratch; use kf_relmse");
+        return KF_ERR_LIMIT;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        kf::set_last_error("kf_relmse_noalloc: no current CUDA device");
+        return KF_ERR_NO_DEVICE;
+    }
+    double* scratch = nullptr;
+    {
+        // set-up, once per device with that device current: the host-side name of the
+        // array is not a device address, so ask the runtime for the device address.
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_relmse_scratch);
+            if (e != cudaSuccess || !p) {
+                kf::set_last_error(std::string("kf_relmse_noalloc: cudaGetSymbolAddress failed: ") +
+                                   cudaGetErrorString(e));
+                return KF_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = static_cast<double*>(p);
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    const uint32_t blocks = (uint32_t)((num_pixels + kNoAllocPixelsPerBlock - 1) / kNoAllocPixelsPerBlock);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // every partial in [0, blocks) and the result slot are written before they are read,
+    // so nothing needs clearing between calls
+    kf::k_relmse_partial<<<blocks, 256, 0, st>>>(reinterpret_cast<const float4*>(x_dev),
+                                                  reinterpret_cast<const float4*>(ref_dev), num_pixels, eps,
+                                                  scratch);
+    kf::k_relmse_final<<<1, 256, 0, st>>>(scratch, blocks, num_pixels, scratch + kNoAllocMaxBlocks);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, scratch + kNoAllocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        kf::set_last_error(std::string("kf_relmse_noalloc: ") + cudaGetErrorString(e));
+        return KF_ERR_CUDA;
+    }
+    return KF_OK;
+}
