@@ -105,6 +105,8 @@ def build_scene(device: int, profile=False, debug=False):
     cfg._c.device = device
     cfg.setProfile(profile)
     cfg.setDebugOutputs(debug)
+    if "traversal" in WORKLOAD:
+        cfg.setTraversal(WORKLOAD["traversal"])
     r = api.Kuafu(cfg)
     cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
                             level=WORKLOAD["level"], seed=WORKLOAD["seed"])
@@ -326,7 +328,10 @@ def main():
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--quick", action="store_true",
                     help="profiling: timed steps only (no e2e, counting or CPU-baseline passes)")
+    ap.add_argument("--traversal", type=int, default=None, help="0: thread per ray, 1: dynamic fetch (default)")
     args = ap.parse_args()
+    if args.traversal is not None:
+        WORKLOAD["traversal"] = args.traversal
     if args.warmup < 3:
         args.warmup = 3
     if args.width:

@@ -82,6 +82,8 @@ typedef struct kf_config {
     uint32_t device;               /* CUDA device ordinal (default 0) */
     uint32_t host_only;            /* 1: scene management and export only, no device is touched;
                                       rendering calls then fail with KF_ERR_NO_DEVICE */
+    uint32_t traversal;            /* 0: one thread per ray; 1: persistent warps with dynamic
+                                      ray fetch (default). Both give identical results. */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */

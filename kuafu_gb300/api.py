@@ -69,6 +69,7 @@ class Config:
     def setTlasLeafSize(self, n): self._c.tlas_leaf_size = int(n)
     def setMaxPathsInFlight(self, n): self._c.max_paths_in_flight = int(n)
     def setHostOnly(self, flag): self._c.host_only = int(bool(flag))
+    def setTraversal(self, mode): self._c.traversal = int(mode)
 
 
 @dataclass

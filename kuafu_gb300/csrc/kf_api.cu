@@ -194,6 +194,8 @@ KF_API void kf_config_init(kf_config* c) {
     c->profile = 0;
     c->use_graph = 1;
     c->device = 0;
+    c->host_only = 0;
+    c->traversal = 1;
 }
 
 KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
@@ -221,6 +223,7 @@ KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
         // persistent grids: enough resident warps to hide traversal latency
         r->grid_extend = (uint32_t)r->num_sms * 16;
         r->grid_shade = (uint32_t)r->num_sms * 8;
+        if (!r->cfg.host_only) r->grid_dyn = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm();
         // Kuafu::Kuafu (kuafu.cpp:27-63): a scene with a 1x1 camera; present mode adds
         // a camera of the initial size and makes it current.
         kf_scene_s* s = new_scene(r.get());

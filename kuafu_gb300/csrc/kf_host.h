@@ -143,7 +143,7 @@ struct kf_renderer_s {
     kf::DeviceBuffer<double> scratch64;
     kf_stats stats{};
     bool count_traversal = false;
-    uint32_t grid_extend = 0, grid_shade = 0;
+    uint32_t grid_extend = 0, grid_shade = 0, grid_dyn = 0;
     // CUDA graph of one frame's launch sequence
     cudaGraphExec_t graph_exec = nullptr;
     std::string graph_key;

@@ -201,7 +201,7 @@ void ensure_wave(kf_renderer_s* r, uint32_t chunk, uint32_t slots, uint64_t npat
         W.radiance_cap = npaths;
     }
     if (r->cfg.debug_outputs && W.primary.count < npaths) W.primary.resize(npaths, st);
-    if (W.counters.count == 0) W.counters.resize(4, st);
+    if (W.counters.count == 0) W.counters.resize(8, st);
     if (W.stats.count == 0) {
         W.stats.resize(16, st);
         KF_CUDA_CHECK(cudaMemsetAsync(W.stats.ptr, 0, W.stats.bytes(), st));
@@ -246,14 +246,22 @@ static void enqueue_frame(kf_renderer_s* r, const SceneDev& sv, const WaveDev& w
         launch_raygen(fd, w, start, n, st);
         int cur = 0;
         for (uint32_t depth = 0; depth <= max_depth; ++depth) {
+            const bool dyn = r->cfg.traversal == 1;
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + (cur ^ 1), 0, sizeof(uint32_t), st));
-            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st));
+            // [2] shadow queue count, [3] / [4] dynamic-fetch cursors
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 3 * sizeof(uint32_t), st));
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[0], st));
-            launch_extend(sv, fd, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
+            if (dyn)
+                launch_trace_dyn(sv, fd, w, cur, depth, start, false, r->grid_dyn, r->count_traversal, st);
+            else
+                launch_extend(sv, fd, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[1], st));
             launch_shade(sv, fd, w, cur, depth, start, r->grid_shade, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[2], st));
-            launch_shadow(sv, w, r->grid_extend, r->count_traversal, st);
+            if (dyn)
+                launch_trace_dyn(sv, fd, w, cur, depth, start, true, r->grid_dyn, r->count_traversal, st);
+            else
+                launch_shadow(sv, w, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[3], st));
             launch_gather(sv, fd, w, cur, start, r->grid_shade, st);
             if (profile) {
@@ -332,7 +340,8 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
         std::snprintf(key, sizeof(key), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u", (void*)s, (void*)c,
                       (unsigned long long)s->gpu.generation, npix, spp, r->cfg.path_depth,
                       (unsigned long long)npaths, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)w.contrib,
-                      (void*)c->accum.ptr, (void*)w.primary, sv.num_slots, r->cfg.russian_roulette);
+                      (void*)c->accum.ptr, (void*)w.primary, sv.num_slots,
+                      r->cfg.russian_roulette | (r->cfg.traversal << 1));
         if (!r->graph_exec || r->graph_key != key) {
             if (r->graph_exec) {
                 cudaGraphExecDestroy(r->graph_exec);

@@ -192,6 +192,11 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         verts.resize(nv * 3);
         idx.reserve(nt * 3);
         mat.reserve(nt);
+        // traversal stack entries address leaves as 26-bit triangle offsets with a 4-bit count
+        KF_REQUIRE(nt < (1ull << 26), KF_ERR_LIMIT, "a scene holds at most 67108863 triangles");
+        KF_REQUIRE(r->cfg.blas_leaf_size >= 1 && r->cfg.blas_leaf_size <= 16, KF_ERR_INVALID_ARGUMENT,
+                   "blas_leaf_size must be in [1, 16]");
+        KF_REQUIRE(s->instances.size() < (1ull << 30), KF_ERR_LIMIT, "too many instances");
         size_t vo = 0, to = 0;
         for (size_t gi = 0; gi < ng; ++gi) {
             const kf_geometry_s* g = s->geometries[gi];

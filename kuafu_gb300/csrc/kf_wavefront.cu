@@ -29,6 +29,7 @@ constexpr uint32_t kMiss = 0xFFFFFFFFu;
 constexpr int kStack = 96;
 constexpr uint32_t kInstTag = 0x80000000u;
 constexpr uint32_t kPopTag = 0xC0000000u;
+constexpr uint32_t kLeafTag = 0x40000000u;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 struct HitOut {
@@ -58,32 +59,88 @@ __device__ __forceinline__ bool anyhit_accept(const SceneDev& s, uint32_t geomet
     return true;
 }
 
-template <bool SHADOW, bool COUNT>
-__device__ bool trace(const SceneDev& s, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
-                      float tmax, HitOut& h, TraceCounters& cnt, AnyHitCtx* ah = nullptr) {
-    h.inst = kMiss;
-    h.t = h.u = h.v = 0.0f;
-    h.prim = 0;
-    if (!s.has_tlas) return false;
-    PRay wr;
-    wr.ox = ox; wr.oy = oy; wr.oz = oz;
-    wr.dx = dx; wr.dy = dy; wr.dz = dz;
-    prep_ray(wr);
-    PRay r = wr;
-    uint32_t stack[kStack];
-    int sp = 0;
-    stack[sp++] = 0;
-    bool in_blas = false;
-    uint32_t cur_inst = 0;
-    uint32_t cur_geom = 0;
-    bool cur_opaque = true;
-    float best = tmax;
-    while (sp > 0) {
-        const uint32_t e = stack[--sp];
+// Traversal stack of one thread: the first kSmemStack entries live in shared
+// memory laid out entry-major (entry * blockDim + thread, so a warp's accesses hit
+// 32 different banks whatever each lane's depth), deeper entries in local memory.
+constexpr int kSmemStack = 40;
+constexpr int kThreadsTrace = 128;
+struct TStack {
+    uint32_t* sm; // &shared[threadIdx.x]
+    uint32_t deep[kStack - kSmemStack];
+    __device__ __forceinline__ void put(int i, uint32_t v) {
+        if (i < kSmemStack)
+            sm[i * kThreadsTrace] = v;
+        else
+            deep[i - kSmemStack] = v;
+    }
+    __device__ __forceinline__ uint32_t get(int i) const {
+        return i < kSmemStack ? sm[i * kThreadsTrace] : deep[i - kSmemStack];
+    }
+};
+
+// Resumable two-level traversal state: init() then step() until it returns true.
+// One step processes one stack entry (a node with its leaf children, an instance
+// entry or the return to the TLAS), so a warp can interleave rays step by step.
+template <bool SHADOW, bool COUNT> struct Tracer {
+    PRay wr, r;
+    TStack stack;
+    int sp;
+    bool in_blas, cur_opaque;
+    uint32_t cur_inst, cur_geom;
+    float tmin, best;
+    HitOut h;
+    TraceCounters cnt;
+
+    __device__ __forceinline__ void init(const SceneDev& s, float ox, float oy, float oz, float dx, float dy,
+                                         float dz, float tmin_, float tmax_) {
+        h.inst = kMiss;
+        h.t = h.u = h.v = 0.0f;
+        h.prim = 0;
+        wr.ox = ox; wr.oy = oy; wr.oz = oz;
+        wr.dx = dx; wr.dy = dy; wr.dz = dz;
+        prep_ray(wr);
+        r = wr;
+        sp = 0;
+        if (s.has_tlas) stack.put(sp++, 0);
+        in_blas = false;
+        cur_inst = cur_geom = 0;
+        cur_opaque = true;
+        tmin = tmin_;
+        best = tmax_;
+    }
+
+    // Returns true when the traversal is over (stack empty, or the first hit of a shadow ray).
+    // Stack entries: kPopTag (back to the TLAS), kInstTag | instance, kLeafTag | (n-1) << 26 |
+    // first triangle (a BLAS leaf of n triangles), or a node index.
+    __device__ __forceinline__ bool step(const SceneDev& s, AnyHitCtx* ah) {
+        if (sp <= 0) return true;
+        const uint32_t e = stack.get(--sp);
         if (e == kPopTag) {
             in_blas = false;
             r = wr;
-            continue;
+            return sp <= 0;
+        }
+        if ((e & 0xC0000000u) == kLeafTag) {
+            const uint32_t first = e & 0x03FFFFFFu, cnt_tri = ((e >> 26) & 0xFu) + 1u;
+#pragma unroll 1
+            for (uint32_t q = 0; q < cnt_tri; ++q) {
+                const float4* tp = reinterpret_cast<const float4*>(s.tris + first + q);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                if (COUNT) cnt.tris++;
+                float t, u, v;
+                if (!intersect_tri(r, a, b, cc, tmin, best, t, u, v)) continue;
+                const uint32_t prim = __float_as_uint(a.w);
+                if (SHADOW) {
+                    h.inst = cur_inst;
+                    sp = 0;
+                    return true;
+                }
+                if (!closer(t, cur_inst, prim, h.t, h.inst, h.prim)) continue;
+                if (!cur_opaque && ah && !anyhit_accept(s, cur_geom, prim, *ah)) continue;
+                h.t = t; h.u = u; h.v = v; h.inst = cur_inst; h.prim = prim;
+                best = t;
+            }
+            return sp <= 0;
         }
         if (e & kInstTag) {
             cur_inst = e & ~kInstTag;
@@ -94,73 +151,81 @@ __device__ bool trace(const SceneDev& s, float ox, float oy, float oz, float dx,
             in.w2o2 = __ldg(&ip->w2o2);
             const uint4 meta = __ldg(reinterpret_cast<const uint4*>(ip) + 3);
             if (COUNT) cnt.insts++;
-            if (meta.z & 2u) continue; // hidden (dummy BLAS, rt.cpp:156)
+            if (meta.z & 2u) return sp <= 0; // hidden (dummy BLAS, rt.cpp:156)
             cur_geom = meta.y;
             cur_opaque = (meta.z & 1u) != 0;
             to_object(in, wr.ox, wr.oy, wr.oz, wr.dx, wr.dy, wr.dz, r);
             in_blas = true;
-            if (sp + 2 > kStack) continue;
-            stack[sp++] = kPopTag;
-            stack[sp++] = meta.x;
-            continue;
+            if (sp + 2 > kStack) return sp <= 0;
+            stack.put(sp++, kPopTag);
+            stack.put(sp++, meta.x);
+            return false;
         }
         const Node4 n = load_node(in_blas ? s.blas_nodes : s.tlas_nodes, e);
         if (COUNT) cnt.nodes++;
         float tn[4];
         const int mask = box4(r, n, tmin, best, tn);
-        uint32_t ic[4];
+        // children to visit, as (entry distance, stack entry); misses get -inf
         float it[4];
-        int k = 0;
+        uint32_t ic[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            if (!(mask & (1 << c))) continue;
             const int cn = lanei(n.cnt, c);
-            const int ch = lanei(n.child, c);
-            if (cn == 0) {
-                ic[k] = (uint32_t)ch;
-                it[k] = tn[c];
-                ++k;
-            } else if (cn > 0) {
+            const uint32_t ch = (uint32_t)lanei(n.child, c);
+            const bool hit = (mask >> c) & 1;
+            it[c] = __int_as_float(0xff800000);
+            ic[c] = 0;
+            if (hit && cn == 0) {
+                it[c] = tn[c];
+                ic[c] = ch;
+            } else if (hit && cn > 0) {
                 if (in_blas) {
-                    for (int q = 0; q < cn; ++q) {
-                        const float4* tp = reinterpret_cast<const float4*>(s.tris + ch + q);
-                        const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-                        if (COUNT) cnt.tris++;
-                        float t, u, v;
-                        if (!intersect_tri(r, a, b, cc, tmin, best, t, u, v)) continue;
-                        const uint32_t prim = __float_as_uint(a.w);
-                        if (SHADOW) {
-                            h.inst = cur_inst;
-                            return true;
-                        }
-                        if (!closer(t, cur_inst, prim, h.t, h.inst, h.prim)) continue;
-                        if (!cur_opaque && ah && !anyhit_accept(s, cur_geom, prim, *ah)) continue;
-                        h.t = t; h.u = u; h.v = v; h.inst = cur_inst; h.prim = prim;
-                        best = t;
-                    }
+                    it[c] = tn[c];
+                    ic[c] = kLeafTag | ((uint32_t)(cn - 1) << 26) | ch;
                 } else {
-                    for (int q = 0; q < cn; ++q) {
-                        if (sp < kStack) stack[sp++] = kInstTag | __ldg(s.tlas_inst + ch + q);
-                    }
+#pragma unroll 1
+                    for (int q = 0; q < cn; ++q)
+                        if (sp < kStack) stack.put(sp++, kInstTag | __ldg(s.tlas_inst + ch + q));
                 }
             }
         }
-        // push inner children far-to-near so the nearest is popped first
-        for (int a = 1; a < k; ++a) {
-            const float tv = it[a];
-            const uint32_t cv = ic[a];
-            int b = a - 1;
-            while (b >= 0 && it[b] < tv) {
-                it[b + 1] = it[b];
-                ic[b + 1] = ic[b];
-                --b;
-            }
-            it[b + 1] = tv;
-            ic[b + 1] = cv;
-        }
-        for (int a = 0; a < k; ++a)
-            if (sp < kStack) stack[sp++] = ic[a];
+        // sort descending by entry distance (fixed network, registers only), then push:
+        // the nearest child ends on top of the stack
+#define KF_CSWAP(a, b)                                                                                     \
+    if (it[a] < it[b]) {                                                                                   \
+        const float tf = it[a];                                                                            \
+        it[a] = it[b];                                                                                     \
+        it[b] = tf;                                                                                        \
+        const uint32_t tu = ic[a];                                                                         \
+        ic[a] = ic[b];                                                                                     \
+        ic[b] = tu;                                                                                        \
     }
+        KF_CSWAP(0, 1)
+        KF_CSWAP(2, 3)
+        KF_CSWAP(0, 2)
+        KF_CSWAP(1, 3)
+        KF_CSWAP(1, 2)
+#undef KF_CSWAP
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (it[c] != __int_as_float(0xff800000) && sp < kStack) stack.put(sp++, ic[c]);
+        return sp <= 0;
+    }
+};
+
+// smem: the block's shared stack area (kSmemStack * kThreadsTrace words).
+template <bool SHADOW, bool COUNT>
+__device__ bool trace(const SceneDev& s, uint32_t* smem, float ox, float oy, float oz, float dx, float dy, float dz,
+                      float tmin, float tmax, HitOut& h, TraceCounters& cnt, AnyHitCtx* ah = nullptr) {
+    Tracer<SHADOW, COUNT> t;
+    t.stack.sm = smem + threadIdx.x;
+    t.init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
+    t.cnt = cnt;
+#pragma unroll 1
+    while (!t.step(s, ah)) {
+    }
+    cnt = t.cnt;
+    h = t.h;
     return h.inst != kMiss;
 }
 
@@ -254,6 +319,7 @@ __global__ void k_raygen(const FrameDev* __restrict__ fp, WaveDev w, uint64_t ch
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
                                                 uint32_t depth, uint64_t chunk_start) {
+    __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = w.counters[cur];
     const float4* __restrict__ qo = w.q_o[cur];
     const float4* __restrict__ qd = w.q_d[cur];
@@ -269,7 +335,7 @@ __global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __re
         AnyHitCtx ah;
         ah.pk = &pk;
         ah.st.init(depth, KF_RNG_ANYHIT);
-        trace<false, COUNT>(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h, cnt, &ah);
+        trace<false, COUNT>(s, s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h, cnt, &ah);
         w.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
         w.hit_prim[i] = h.prim;
         if (depth == 0 && w.primary) {
@@ -762,13 +828,14 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
 // ---------------------------------------------------------------------------
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_shadow(SceneDev s, WaveDev w) {
+    __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = w.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[2], (unsigned long long)count);
     TraceCounters cnt{0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const float4 o = w.sq_o[i], d = w.sq_d[i];
         HitOut h;
-        const bool occluded = trace<true, COUNT>(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w, h, cnt);
+        const bool occluded = trace<true, COUNT>(s, s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w, h, cnt);
         if (!occluded) {
             const uint32_t tag = __float_as_uint(d.w);
             const uint32_t slot = tag >> 26, p = tag & ((1u << 26) - 1u);
@@ -779,6 +846,98 @@ __global__ void __launch_bounds__(128) k_shadow(SceneDev s, WaveDev w) {
         atomicAdd(&w.stats[6], (unsigned long long)cnt.nodes);
         atomicAdd(&w.stats[7], (unsigned long long)cnt.tris);
         atomicAdd(&w.stats[8], (unsigned long long)cnt.insts);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent traversal with dynamic ray fetch. Each warp keeps up to 32 rays in
+// flight; whenever fewer than kRefillBelow lanes are busy, the idle lanes take
+// the next rays of the queue (one ballot, one atomic per warp), so a warp does
+// not idle behind its slowest ray. Results are identical to k_extend / k_shadow:
+// each ray runs the same Tracer steps, only the interleaving changes.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kRefillBelow = 24;
+constexpr int kStepsPerRefill = 8;
+
+template <bool SHADOW, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
+                                                   uint32_t depth, uint64_t chunk_start) {
+    __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
+    const uint32_t count = SHADOW ? w.counters[2] : w.counters[cur];
+    uint32_t* fetch = w.counters + (SHADOW ? 4 : 3);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(&w.stats[SHADOW ? 2 : (depth == 0 ? 0 : 1)], (unsigned long long)count);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t npix = fp->npix;
+    Tracer<SHADOW, COUNT> t;
+    t.stack.sm = s_stack + threadIdx.x;
+    t.cnt = TraceCounters{0, 0, 0};
+    PathKey pk{make_uint2(0, 0), 0, 0};
+    AnyHitCtx ah;
+    ah.pk = &pk;
+    ah.st.init(depth, KF_RNG_ANYHIT);
+    bool active = false;
+    bool exhausted = false;
+    uint32_t idx = 0;
+    for (;;) {
+        uint32_t act = __ballot_sync(kFull, active);
+        if (!exhausted && (uint32_t)__popc(act) < kRefillBelow) {
+            const bool need = !active;
+            const uint32_t m = __ballot_sync(kFull, need);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(fetch, (uint32_t)__popc(m));
+            base = __shfl_sync(kFull, base, 0);
+            if (base + (uint32_t)__popc(m) >= count) exhausted = true;
+            if (need) {
+                const uint32_t j = base + __popc(m & lanemask_lt());
+                if (j < count) {
+                    idx = j;
+                    if (SHADOW) {
+                        const float4 o = w.sq_o[j], d = w.sq_d[j];
+                        t.init(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w);
+                    } else {
+                        const float4 o = w.q_o[cur][j], d = w.q_d[cur][j];
+                        const uint64_t g = chunk_start + __float_as_uint(o.w);
+                        pk = PathKey{make_uint2(fp->seed ^ (uint32_t)(g % npix), fp->camera_index),
+                                     (uint32_t)(g / npix), fp->frame};
+                        ah.st.init(depth, KF_RNG_ANYHIT);
+                        t.init(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX);
+                    }
+                    active = true;
+                }
+            }
+            act = __ballot_sync(kFull, active);
+        }
+        if (act == 0) break;
+        if (active) {
+            bool done = false;
+#pragma unroll 1
+            for (int k = 0; k < kStepsPerRefill && !done; ++k) done = t.step(s, SHADOW ? nullptr : &ah);
+            if (done) {
+                if (SHADOW) {
+                    if (t.h.inst == kMiss) {
+                        const uint32_t tag = __float_as_uint(w.sq_d[idx].w);
+                        w.vis[(size_t)(tag >> 26) * w.chunk_cap + (tag & ((1u << 26) - 1u))] = 1;
+                    }
+                } else {
+                    w.hit[idx] = make_float4(t.h.t, t.h.u, t.h.v, __uint_as_float(t.h.inst));
+                    w.hit_prim[idx] = t.h.prim;
+                    if (depth == 0 && w.primary) {
+                        const uint32_t p = __float_as_uint(w.q_o[cur][idx].w);
+                        kf_hit ph;
+                        ph.t = t.h.t; ph.u = t.h.u; ph.v = t.h.v; ph.instance = t.h.inst; ph.prim = t.h.prim;
+                        ph.pad[0] = ph.pad[1] = ph.pad[2] = 0;
+                        w.primary[chunk_start + p] = ph;
+                    }
+                }
+                active = false;
+            }
+        }
+    }
+    if (COUNT) {
+        warp_add_stat(&w.stats[SHADOW ? 6 : 3], t.cnt.nodes);
+        warp_add_stat(&w.stats[SHADOW ? 7 : 4], t.cnt.tris);
+        warp_add_stat(&w.stats[SHADOW ? 8 : 5], t.cnt.insts);
     }
 }
 
@@ -919,6 +1078,29 @@ void launch_shadow(const SceneDev& s, const WaveDev& w, uint32_t grid, bool coun
         k_shadow<false><<<grid, 128, 0, st>>>(s, w);
     KF_CUDA_CHECK(cudaGetLastError());
 }
+void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
+                      uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode, cudaStream_t st) {
+    if (shadow) {
+        if (count_mode)
+            k_trace_dyn<true, true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+        else
+            k_trace_dyn<true, false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+    } else {
+        if (count_mode)
+            k_trace_dyn<false, true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+        else
+            k_trace_dyn<false, false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+    }
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+
+uint32_t trace_dyn_blocks_per_sm() {
+    int a = 0, b = 0;
+    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<false, false>, 128, 0));
+    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_dyn<true, false>, 128, 0));
+    return (uint32_t)std::max(1, std::min(a, b));
+}
+
 void launch_gather(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint64_t chunk_start,
                    uint32_t grid, cudaStream_t st) {
     k_gather<<<grid, 256, 0, st>>>(s, f, w, cur, chunk_start);

@@ -74,6 +74,11 @@ void launch_extend(const SceneDev& s, const FrameDev* f, const WaveDev& w, int c
 void launch_shade(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
                   uint64_t chunk_start, uint32_t grid, cudaStream_t st);
 void launch_shadow(const SceneDev& s, const WaveDev& w, uint32_t grid, bool count_mode, cudaStream_t st);
+// Persistent traversal with dynamic ray fetch (closest hit, or shadow rays when `shadow`).
+// Needs w.counters[3] (closest) / w.counters[4] (shadow) zeroed before the launch.
+void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
+                      uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode, cudaStream_t st);
+uint32_t trace_dyn_blocks_per_sm();
 void launch_gather(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint64_t chunk_start,
                    uint32_t grid, cudaStream_t st);
 void launch_resolve(const FrameDev* f, const float4* radiance, uint32_t npix, uint32_t spp, float4* accum,

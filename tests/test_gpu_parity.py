@@ -102,13 +102,15 @@ def test_frame_accumulation_and_srgb_frame():
         assert (s64[..., 3] == 3.0).all()
 
 
-def test_icospheres_with_lights_bvh_parity():
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_icospheres_with_lights_bvh_parity(traversal):
     """Two-level traversal over many BLAS, PrincipledBSDF lobes incl. transmission, NEE over
-    directional / point / spot lights, Russian roulette."""
+    directional / point / spot lights, Russian roulette; both traversal kernels."""
     spp, depth = 2, 4
     cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
     cfg.setDebugOutputs(True)
     cfg.setRussianRouletteMinBounces(1)
+    cfg.setTraversal(traversal)
     with api.Kuafu(cfg) as r:
         cam = scenes.icospheres(r, 96, 64, count=24, level=2)
         paths, hits, rgba, ref = _render_pair(r, cam, spp, depth, rr=True, rr_min=1, clear=(0.1, 0.1, 0.1, 1.0),
