@@ -249,6 +249,18 @@ typedef struct kf_batch_item {
 } kf_batch_item;
 KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint32_t count);
 
+/* ---- tensor-core building blocks of the learned denoiser (device pointers; no
+ * counterpart in kuafu, whose OptiX denoiser is closed code, denoiser.cpp:257-316) ---- */
+/* y[n,y,x,y_coff+co] = act(bias[co] + sum x[n,y+dy,x+dx,ci] * w[tap][co][ci]), NHWC BF16,
+ * zero padding, FP32 accumulation; w: [9][w_rows][cin], w_rows % 16 == 0, cin % 32 == 0. */
+KF_API int kf_conv3x3_bf16(const void* x, int n, int h, int w, int cin, const void* weight, int w_rows,
+                           const float* bias, int cout, int relu, void* y, int y_cstride, int y_coff, void* stream);
+/* d[m][n] += sum_k a[m][k] * b[n][k], BF16 K-major operands, FP32 accumulation (split-K atomics). */
+KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, float* d, int ldd, int splits,
+                           void* stream);
+/* Error word of the tensor-core kernels (0 = none; set when a bounded wait expired); cleared on read. */
+KF_API int kf_tc_error(uint32_t* out);
+
 /* ---- FP64 relative-MSE reduction: mean over pixels and channels of
  * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64 ---- */
 KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,

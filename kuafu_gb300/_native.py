@@ -213,6 +213,9 @@ PROTOTYPES = {
     "kf_renderer_run_batch": (I, [VP, C.POINTER(kf_batch_item), U32]),
     "kf_relmse": (I, [VP, VP, VP, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
     "kf_relmse_noalloc": (I, [VP, VP, C.c_uint64, C.c_double, VP, C.POINTER(C.c_double)]),
+    "kf_conv3x3_bf16": (I, [VP, I, I, I, I, VP, I, VP, I, I, VP, I, I, VP]),
+    "kf_gemm_bf16_tn": (I, [VP, I, VP, I, I, VP, I, I, VP]),
+    "kf_tc_error": (I, [C.POINTER(U32)]),
 }
 
 KF_AOV_RADIANCE_F32, KF_AOV_ALBEDO_F32, KF_AOV_NORMAL_F32, KF_AOV_DEPTH_F32 = 0, 1, 2, 3

@@ -36,6 +36,7 @@ SOURCES = [
     ("kf_render.cu", ["-fmad=false"]),
     ("kf_bvh.cu", ["-fmad=false"]),
     ("kf_wavefront.cu", ["-fmad=false"]),
+    ("kf_conv.cu", []),
     ("kf_mesh.cpp", []),
 ]
 

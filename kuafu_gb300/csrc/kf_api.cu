@@ -1016,3 +1016,32 @@ KF_API int kf_relmse(kf_renderer r, const float* x, const float* ref, uint64_t n
 }
 
 } // extern "C"
+
+// ---- tensor-core building blocks (kf_conv.cu) ----
+#include "kf_conv.h"
+
+extern "C" {
+KF_API int kf_conv3x3_bf16(const void* x, int n, int h, int w, int cin, const void* weight, int w_rows,
+                           const float* bias, int cout, int relu, void* y, int y_cstride, int y_coff, void* stream) {
+    return guarded([&] {
+        REQ(x && weight && y, "null tensor");
+        conv3x3_bf16(static_cast<const __nv_bfloat16*>(x), n, h, w, cin, static_cast<const __nv_bfloat16*>(weight),
+                     w_rows, bias, cout, relu != 0, static_cast<__nv_bfloat16*>(y), y_cstride, y_coff,
+                     static_cast<cudaStream_t>(stream));
+    });
+}
+KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, float* d, int ldd, int splits,
+                           void* stream) {
+    return guarded([&] {
+        REQ(a && b && d, "null tensor");
+        gemm_bf16_tn(static_cast<const __nv_bfloat16*>(a), m, static_cast<const __nv_bfloat16*>(b), n, k, d, ldd,
+                     splits, static_cast<cudaStream_t>(stream));
+    });
+}
+KF_API int kf_tc_error(uint32_t* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        *out = tc_take_error();
+    });
+}
+}
