@@ -261,6 +261,45 @@ KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, fl
 /* Error word of the tensor-core kernels (0 = none; set when a bounded wait expired); cleared on read. */
 KF_API int kf_tc_error(uint32_t* out);
 
+/* ---- learned denoiser: replaces kuafu's OptiX pass (Config::setUseDenoiser,
+ * config.cpp:142; context.cpp:651-670 feeds rgba + albedo + normal to OptiX and
+ * writes the result back over the presented image). Here a U-Net (3x3 convs,
+ * 32/64/96/128/160 channels) over log radiance, albedo, normal and depth,
+ * trained on this renderer's own low-spp / high-spp pairs. ---- */
+typedef struct kf_denoiser_s* kf_denoiser;
+/* A denoiser with He-initialised weights (seeded). Destroy it before its renderer. */
+KF_API int kf_denoiser_create(kf_renderer r, uint32_t seed, kf_denoiser* out);
+KF_API int kf_denoiser_destroy(kf_denoiser d);
+KF_API int kf_denoiser_num_params(kf_denoiser d, uint64_t* out);
+/* FP32 master parameters (per conv: weights [9][cout][cin] then bias [cout]), host memory. */
+KF_API int kf_denoiser_get_params(kf_denoiser d, float* out, uint64_t count);
+KF_API int kf_denoiser_set_params(kf_denoiser d, const float* in, uint64_t count); /* resets Adam state */
+KF_API int kf_denoiser_save(kf_denoiser d, const char* path);
+KF_API int kf_denoiser_load(kf_denoiser d, const char* path);
+/* Renders one training pair with camera c of scene s: one frame of low_spp samples
+ * (the input) and the running mean of high_frames frames of high_spp (the target).
+ * Width and height divisible by 16; all views of a denoiser share one size. */
+KF_API int kf_denoiser_add_view(kf_denoiser d, kf_scene s, kf_camera c, uint32_t low_spp, uint32_t high_spp,
+                                uint32_t high_frames);
+KF_API int kf_denoiser_num_views(kf_denoiser d, uint32_t* out);
+/* iters Adam steps over batch random crops (crop x crop, crop % 16 == 0); *mean_loss may be NULL. */
+KF_API int kf_denoiser_train(kf_denoiser d, uint32_t iters, uint32_t batch, uint32_t crop, float lr,
+                             float* mean_loss);
+/* Denoises camera c's accumulated radiance into its KF_AOV_DENOISED_F32 target. */
+KF_API int kf_denoiser_apply(kf_denoiser d, kf_camera c);
+/* Attach (or detach with NULL) the denoiser that kf_renderer_run uses when the config's
+ * use_denoiser is set: the presented frame (kf_renderer_download_latest_frame) is then
+ * the denoised radiance; the accumulation target itself is left untouched. */
+KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d);
+/* Tensor-level entry points (device pointers, stream = the renderer's):
+ * feat [n][h][w][32] BF16 network input, out [n][h][w][32] BF16 (channels 0..2 =
+ * log1p radiance), target [n][h][w] float4 linear radiance; h, w % 16 == 0.
+ * train_step computes loss and gradients (copied to grads_dev, may be NULL, FP32,
+ * num_params) and, if apply, one Adam step with learning rate lr. */
+KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, int n, int h, int w, void* out);
+KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* target, int n, int h, int w,
+                                  float lr, float* grads_dev, int apply, float* loss);
+
 /* ---- FP64 relative-MSE reduction: mean over pixels and channels of
  * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64 ---- */
 KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,

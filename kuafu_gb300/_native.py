@@ -216,6 +216,20 @@ PROTOTYPES = {
     "kf_conv3x3_bf16": (I, [VP, I, I, I, I, VP, I, VP, I, I, VP, I, I, VP]),
     "kf_gemm_bf16_tn": (I, [VP, I, VP, I, I, VP, I, I, VP]),
     "kf_tc_error": (I, [C.POINTER(U32)]),
+    "kf_denoiser_create": (I, [VP, U32, C.POINTER(VP)]),
+    "kf_denoiser_destroy": (I, [VP]),
+    "kf_denoiser_num_params": (I, [VP, C.POINTER(C.c_uint64)]),
+    "kf_denoiser_get_params": (I, [VP, VP, C.c_uint64]),
+    "kf_denoiser_set_params": (I, [VP, VP, C.c_uint64]),
+    "kf_denoiser_save": (I, [VP, C.c_char_p]),
+    "kf_denoiser_load": (I, [VP, C.c_char_p]),
+    "kf_denoiser_add_view": (I, [VP, VP, VP, U32, U32, U32]),
+    "kf_denoiser_num_views": (I, [VP, C.POINTER(U32)]),
+    "kf_denoiser_train": (I, [VP, U32, U32, U32, F, C.POINTER(F)]),
+    "kf_denoiser_apply": (I, [VP, VP]),
+    "kf_renderer_set_denoiser": (I, [VP, VP]),
+    "kf_denoiser_forward": (I, [VP, VP, I, I, I, VP]),
+    "kf_denoiser_train_step": (I, [VP, VP, VP, I, I, I, F, VP, I, C.POINTER(F)]),
 }
 
 KF_AOV_RADIANCE_F32, KF_AOV_ALBEDO_F32, KF_AOV_NORMAL_F32, KF_AOV_DEPTH_F32 = 0, 1, 2, 3

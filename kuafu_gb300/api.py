@@ -10,6 +10,7 @@ throws std::runtime_error).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -476,6 +477,80 @@ class Kuafu:
             arr[i].camera = cam._h.value
             arr[i].spp = int(spp)
         N.check(_lib().kf_renderer_run_batch(self._h, arr, len(items)))
+
+    def setDenoiser(self, denoiser: "Denoiser | None"):
+        """Denoiser that run() applies when the config's use_denoiser is set."""
+        N.check(_lib().kf_renderer_set_denoiser(self._h, denoiser._h if denoiser else None))
+
+
+class Denoiser:
+    """Learned U-Net denoiser: stands in for kuafu's OptiX pass (Config::setUseDenoiser,
+    src/core/config.cpp:142; src/core/context/context.cpp:651-670), trained on this
+    renderer's own low-spp / high-spp pairs. All work runs on the renderer's stream."""
+
+    def __init__(self, renderer: Kuafu, seed: int = 0):
+        h = C.c_void_p()
+        N.check(_lib().kf_denoiser_create(renderer._h, int(seed), C.byref(h)))
+        self._h = h
+        self.renderer = renderer
+
+    def close(self):
+        if self._h:
+            N.check(_lib().kf_denoiser_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def numParams(self) -> int:
+        n = C.c_uint64()
+        N.check(_lib().kf_denoiser_num_params(self._h, C.byref(n)))
+        return n.value
+
+    def getParams(self) -> np.ndarray:
+        out = np.empty(self.numParams(), np.float32)
+        N.check(_lib().kf_denoiser_get_params(self._h, out.ctypes.data, out.size))
+        return out
+
+    def setParams(self, p: np.ndarray):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        N.check(_lib().kf_denoiser_set_params(self._h, a.ctypes.data, a.size))
+
+    def save(self, path):
+        N.check(_lib().kf_denoiser_save(self._h, os.fsencode(path)))
+
+    def load(self, path):
+        N.check(_lib().kf_denoiser_load(self._h, os.fsencode(path)))
+
+    def addView(self, scene: Scene, cam: Camera, low_spp: int, high_spp: int, high_frames: int = 1):
+        N.check(_lib().kf_denoiser_add_view(self._h, scene._h, cam._h, int(low_spp), int(high_spp),
+                                            int(high_frames)))
+
+    def numViews(self) -> int:
+        n = C.c_uint32()
+        N.check(_lib().kf_denoiser_num_views(self._h, C.byref(n)))
+        return n.value
+
+    def train(self, iters: int, batch: int = 8, crop: int = 128, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        N.check(_lib().kf_denoiser_train(self._h, int(iters), int(batch), int(crop), float(lr), C.byref(loss)))
+        return loss.value
+
+    def apply(self, cam: Camera):
+        N.check(_lib().kf_denoiser_apply(self._h, cam._h))
+
+    def forward(self, feat_ptr: int, n: int, h: int, w: int, out_ptr: int):
+        N.check(_lib().kf_denoiser_forward(self._h, feat_ptr, n, h, w, out_ptr))
+
+    def trainStep(self, feat_ptr: int, target_ptr: int, n: int, h: int, w: int, lr: float = 0.0,
+                  grads_ptr: int | None = None, apply: bool = False) -> float:
+        loss = C.c_float()
+        N.check(_lib().kf_denoiser_train_step(self._h, feat_ptr, target_ptr, n, h, w, float(lr), grads_ptr,
+                                              int(bool(apply)), C.byref(loss)))
+        return loss.value
 
 
 def materialCount() -> int:

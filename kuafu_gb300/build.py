@@ -37,6 +37,7 @@ SOURCES = [
     ("kf_bvh.cu", ["-fmad=false"]),
     ("kf_wavefront.cu", ["-fmad=false"]),
     ("kf_conv.cu", []),
+    ("kf_denoise.cu", []),
     ("kf_mesh.cpp", []),
 ]
 

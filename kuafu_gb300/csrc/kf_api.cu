@@ -8,6 +8,7 @@
 #include <new>
 #include <string>
 
+#include "kf_denoise.h"
 #include "kf_host.h"
 
 namespace kf {
@@ -327,7 +328,10 @@ KF_API int kf_renderer_run(kf_renderer r) {
             std::memcpy(r->last_position, c->position, sizeof(r->last_position));
         }
         camera_update_view(c);
+        KF_REQUIRE(!r->cfg.use_denoiser || r->denoiser, KF_ERR_STATE,
+                   "use_denoiser is set but no denoiser is attached (kf_renderer_set_denoiser)");
         render_frame(r, s, c, r->cfg.spp);
+        if (r->cfg.use_denoiser) present_denoised(r, c);
     });
 }
 
@@ -1042,6 +1046,150 @@ KF_API int kf_tc_error(uint32_t* out) {
     return guarded([&] {
         REQ(out, "null argument");
         *out = tc_take_error();
+    });
+}
+}
+
+// ---- learned denoiser (kf_denoise.cu) ----
+#include <cstdio>
+
+namespace {
+constexpr uint32_t kDenoiserMagic = 0x4E44464Bu; // "KFDN"
+constexpr uint32_t kDenoiserVersion = 1;
+
+kf_denoiser_s* check_denoiser(kf_denoiser d) {
+    REQ(d, "invalid denoiser");
+    return d;
+}
+} // namespace
+
+extern "C" {
+KF_API int kf_denoiser_create(kf_renderer r, uint32_t seed, kf_denoiser* out) {
+    return guarded([&] {
+        REQ(r && out, "null argument");
+        require_device(r);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        *out = denoiser_create(r, seed);
+    });
+}
+KF_API int kf_denoiser_destroy(kf_denoiser d) {
+    return guarded([&] {
+        if (!d) return;
+        kf_renderer_s* r = denoiser_renderer(d);
+        if (r->denoiser == d) r->denoiser = nullptr;
+        cudaStreamSynchronize(r->stream);
+        denoiser_destroy(d);
+    });
+}
+KF_API int kf_denoiser_num_params(kf_denoiser d, uint64_t* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        *out = denoiser_num_params(check_denoiser(d));
+    });
+}
+KF_API int kf_denoiser_get_params(kf_denoiser d, float* out, uint64_t count) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        denoiser_get_params(check_denoiser(d), out, count);
+    });
+}
+KF_API int kf_denoiser_set_params(kf_denoiser d, const float* in, uint64_t count) {
+    return guarded([&] {
+        REQ(in, "null argument");
+        denoiser_set_params(check_denoiser(d), in, count);
+    });
+}
+KF_API int kf_denoiser_save(kf_denoiser d, const char* path) {
+    return guarded([&] {
+        REQ(path, "null path");
+        const size_t n = denoiser_num_params(check_denoiser(d));
+        std::vector<float> p(n);
+        denoiser_get_params(d, p.data(), n);
+        FILE* f = std::fopen(path, "wb");
+        KF_REQUIRE(f, KF_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+        const uint32_t hdr[3] = {kDenoiserMagic, kDenoiserVersion, (uint32_t)n};
+        const bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 && std::fwrite(p.data(), 4, n, f) == n;
+        std::fclose(f);
+        KF_REQUIRE(ok, KF_ERR_INTERNAL, std::string("short write to ") + path);
+    });
+}
+KF_API int kf_denoiser_load(kf_denoiser d, const char* path) {
+    return guarded([&] {
+        REQ(path, "null path");
+        const size_t n = denoiser_num_params(check_denoiser(d));
+        FILE* f = std::fopen(path, "rb");
+        KF_REQUIRE(f, KF_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+        uint32_t hdr[3] = {0, 0, 0};
+        std::vector<float> p(n);
+        const bool ok = std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == kDenoiserMagic &&
+                        hdr[1] == kDenoiserVersion && hdr[2] == n && std::fread(p.data(), 4, n, f) == n;
+        std::fclose(f);
+        KF_REQUIRE(ok, KF_ERR_INVALID_ARGUMENT, std::string("not a denoiser parameter file of this network: ") + path);
+        denoiser_set_params(d, p.data(), n);
+    });
+}
+KF_API int kf_denoiser_add_view(kf_denoiser d, kf_scene s, kf_camera c, uint32_t low_spp, uint32_t high_spp,
+                                uint32_t high_frames) {
+    return guarded([&] {
+        check_denoiser(d);
+        kf_scene_s* sc = check_scene(s);
+        kf_camera_s* cam = check_camera(c);
+        REQ(cam->scene == sc, "the camera does not belong to the scene");
+        REQ(low_spp > 0 && high_spp > 0 && high_frames > 0, "sample counts must be positive");
+        kf_renderer_s* r = denoiser_renderer(d);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        camera_update_view(cam);
+        denoiser_add_view(d, sc, cam, low_spp, high_spp, high_frames);
+        r->last_camera = nullptr; // the next run() restarts accumulation
+    });
+}
+KF_API int kf_denoiser_num_views(kf_denoiser d, uint32_t* out) {
+    return guarded([&] {
+        REQ(out, "null argument");
+        *out = denoiser_num_views(check_denoiser(d));
+    });
+}
+KF_API int kf_denoiser_train(kf_denoiser d, uint32_t iters, uint32_t batch, uint32_t crop, float lr,
+                             float* mean_loss) {
+    return guarded([&] {
+        check_denoiser(d);
+        KF_CUDA_CHECK(cudaSetDevice(denoiser_renderer(d)->device));
+        const float l = denoiser_train(d, iters, batch, crop, lr);
+        if (mean_loss) *mean_loss = l;
+    });
+}
+KF_API int kf_denoiser_apply(kf_denoiser d, kf_camera c) {
+    return guarded([&] {
+        check_denoiser(d);
+        kf_camera_s* cam = check_camera(c);
+        kf_renderer_s* r = denoiser_renderer(d);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        denoiser_apply(d, cam);
+        sync_stream(r);
+    });
+}
+KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        REQ(!d || denoiser_renderer(d) == r, "the denoiser belongs to another renderer");
+        r->denoiser = d;
+    });
+}
+KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, int n, int h, int w, void* out) {
+    return guarded([&] {
+        REQ(feat && out && n > 0 && h > 0 && w > 0, "invalid tensor");
+        check_denoiser(d);
+        denoiser_forward(d, feat, n, h, w, out);
+        sync_stream(denoiser_renderer(d));
+    });
+}
+KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* target, int n, int h, int w,
+                                  float lr, float* grads_dev, int apply, float* loss) {
+    return guarded([&] {
+        REQ(feat && target && n > 0 && h > 0 && w > 0, "invalid tensor");
+        check_denoiser(d);
+        const float l = denoiser_train_step(d, feat, target, n, h, w, lr, grads_dev, apply != 0);
+        if (loss) *loss = l;
     });
 }
 }

@@ -149,6 +149,8 @@ struct kf_renderer_s {
     std::string graph_key;
     // events for profiling
     cudaEvent_t ev[8] = {};
+    // learned denoiser used by run() when cfg.use_denoiser is set (not owned)
+    kf_denoiser_s* denoiser = nullptr;
     ~kf_renderer_s();
 };
 

@@ -1,0 +1,242 @@
+"""Learned denoiser: the tcgen05 U-Net against a PyTorch FP32 reference of the same
+network and loss, then training and denoising on rendered Cornell boxes.
+
+Tolerances. The CUDA path keeps activations and activation gradients in BF16 (8
+significant bits) and accumulates in FP32. The forward reference rounds to BF16
+at the same points, so outputs agree to 2e-2 of their scale. Gradients are
+compared with an FP32 autograd reference (no BF16 rounding between layers):
+per layer, cosine similarity >= 0.99 and relative L2 error <= 0.1.
+"""
+import numpy as np
+import pytest
+
+from kuafu_gb300 import _native as N
+from kuafu_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+# (cin, cout, relu) of the 19 convolutions, in parameter order
+LAYERS = [(32, 32, 1), (32, 32, 1), (32, 64, 1), (64, 64, 1), (64, 96, 1), (96, 96, 1), (96, 128, 1),
+          (128, 128, 1), (128, 160, 1), (160, 160, 1), (288, 128, 1), (128, 128, 1), (224, 96, 1), (96, 96, 1),
+          (160, 64, 1), (64, 64, 1), (96, 32, 1), (32, 32, 1), (32, 3, 0)]
+LAMBDA = 0.5
+
+
+def _unpack(params, torch):
+    out, o = [], 0
+    for cin, cout, _ in LAYERS:
+        w = params[o:o + 9 * cout * cin].reshape(9, cout, cin)
+        o += 9 * cout * cin
+        b = params[o:o + cout]
+        o += cout
+        out.append((torch.tensor(w).permute(1, 2, 0).reshape(cout, cin, 3, 3).contiguous(), torch.tensor(b)))
+    assert o == params.size
+    return out
+
+
+def _unet(x, wb, torch, rnd):
+    """x: [n, 32, h, w] -> [n, 3, h, w]; rnd rounds activations (BF16 emulation or identity)."""
+    F = torch.nn.functional
+
+    def conv(i, t):
+        w, b = wb[i]
+        y = F.conv2d(t, w, b, padding=1)
+        return rnd(torch.relu(y) if LAYERS[i][2] else y)
+
+    pool = lambda t: rnd(F.avg_pool2d(t, 2))
+    up = lambda t: F.interpolate(t, scale_factor=2, mode="nearest")
+    e0 = conv(1, conv(0, x))
+    e1 = conv(3, conv(2, pool(e0)))
+    e2 = conv(5, conv(4, pool(e1)))
+    e3 = conv(7, conv(6, pool(e2)))
+    e4 = conv(9, conv(8, pool(e3)))
+    d3 = conv(11, conv(10, torch.cat([up(e4), e3], 1)))
+    d2 = conv(13, conv(12, torch.cat([up(d3), e2], 1)))
+    d1 = conv(15, conv(14, torch.cat([up(d2), e1], 1)))
+    d0 = conv(17, conv(16, torch.cat([up(d1), e0], 1)))
+    return conv(18, d0)
+
+
+def _loss(pred, target, torch):
+    """pred [n, 3, h, w] (log1p space), target [n, h, w, 4] linear."""
+    t = torch.log1p(target[..., :3].clamp_min(0)).permute(0, 3, 1, 2)
+    d = pred - t
+    cnt = d.numel()
+    l1 = d.abs().sum()
+    gx = ((pred[..., 1:] - pred[..., :-1]) - (t[..., 1:] - t[..., :-1])).abs().sum()
+    gy = ((pred[:, :, 1:] - pred[:, :, :-1]) - (t[:, :, 1:] - t[:, :, :-1])).abs().sum()
+    return (l1 + LAMBDA * (gx + gy)) / cnt
+
+
+def _inputs(torch, n, h, w, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    feat = torch.zeros((n, h, w, 32), device="cuda")
+    feat[..., :10] = torch.randn((n, h, w, 10), device="cuda", generator=g)
+    feat = feat.to(torch.bfloat16)
+    target = torch.rand((n, h, w, 4), device="cuda", generator=g) * 3.0
+    return feat, target
+
+
+def _tc_error():
+    import ctypes as C
+    e = C.c_uint32()
+    N.check(N.load().kf_tc_error(C.byref(e)))
+    return e.value
+
+
+@pytest.fixture(scope="module")
+def renderer():
+    with api.Kuafu(scenes.cornell_config(spp=4, depth=5)) as r:
+        yield r
+
+
+def test_forward_matches_torch(renderer):
+    import torch
+
+    d = api.Denoiser(renderer, seed=3)
+    params = d.getParams()
+    wb = [(w.cuda().to(torch.bfloat16).float(), b.cuda()) for w, b in _unpack(params, torch)]
+    n, h, w = 2, 48, 80
+    feat, _ = _inputs(torch, n, h, w, 11)
+    out = torch.zeros((n, h, w, 32), device="cuda", dtype=torch.bfloat16)
+    torch.cuda.synchronize()
+    d.forward(feat.data_ptr(), n, h, w, out.data_ptr())
+    assert _tc_error() == 0
+    rnd = lambda t: t.to(torch.bfloat16).float()
+    ref = _unet(feat.float().permute(0, 3, 1, 2), wb, torch, rnd).permute(0, 2, 3, 1)
+    got = out[..., :3].float()
+    scale = ref.abs().max().item()
+    err = (got - ref).abs().max().item() / scale
+    assert err < 2e-2, f"max error {err:.3e} of scale {scale:.3e}"
+    assert (out[..., 3:] == 0).all()
+    d.close()
+
+
+def test_gradients_match_autograd(renderer):
+    import torch
+
+    d = api.Denoiser(renderer, seed=5)
+    params = d.getParams()
+    # give the decoder some signal: random biases so no layer is dead
+    rng = np.random.default_rng(0)
+    o = 0
+    for cin, cout, _ in LAYERS:
+        o += 9 * cout * cin
+        params[o:o + cout] = rng.normal(0.0, 0.05, cout)
+        o += cout
+    d.setParams(params)
+    n, h, w = 2, 32, 48
+    feat, target = _inputs(torch, n, h, w, 21)
+    grads = torch.zeros(params.size, device="cuda", dtype=torch.float32)
+    torch.cuda.synchronize()
+    loss = d.trainStep(feat.data_ptr(), target.data_ptr(), n, h, w, grads_ptr=grads.data_ptr(), apply=False)
+    torch.cuda.synchronize()
+    assert _tc_error() == 0
+    wb = []
+    for wt, b in _unpack(params, torch):
+        wb.append((wt.cuda().to(torch.bfloat16).float().requires_grad_(True), b.cuda().requires_grad_(True)))
+    pred = _unet(feat.float().permute(0, 3, 1, 2), wb, torch, lambda t: t)
+    ref_loss = _loss(pred, target, torch)
+    ref_loss.backward()
+    assert abs(loss - ref_loss.item()) <= 2e-2 * ref_loss.item(), (loss, ref_loss.item())
+    g = grads.cpu().numpy()
+    o = 0
+    for i, (cin, cout, _) in enumerate(LAYERS):
+        gw = g[o:o + 9 * cout * cin].reshape(9, cout, cin)
+        o += 9 * cout * cin
+        gb = g[o:o + cout]
+        o += cout
+        rw = wb[i][0].grad.reshape(cout, cin, 9).permute(2, 0, 1).cpu().numpy()
+        rb = wb[i][1].grad.cpu().numpy()
+        for got, ref, what in ((gw, rw, "weight"), (gb, rb, "bias")):
+            num = float(np.dot(got.ravel(), ref.ravel()))
+            den = float(np.linalg.norm(got) * np.linalg.norm(ref)) + 1e-30
+            rel = float(np.linalg.norm(got - ref) / (np.linalg.norm(ref) + 1e-30))
+            assert num / den >= 0.99 and rel <= 0.1, f"layer {i} {what}: cos {num / den:.4f} rel {rel:.3e}"
+    d.close()
+
+
+def test_training_reduces_loss(renderer):
+    import torch
+
+    d = api.Denoiser(renderer, seed=7)
+    n, h, w = 4, 64, 64
+    feat, _ = _inputs(torch, n, h, w, 31)
+    # a learnable target: a smooth function of the input channels
+    target = torch.ones((n, h, w, 4), device="cuda")
+    target[..., :3] = torch.expm1(0.5 * torch.relu(feat[..., :3].float()) + 0.2 * feat[..., 3:6].float().abs())
+    torch.cuda.synchronize()
+    first = d.trainStep(feat.data_ptr(), target.data_ptr(), n, h, w, lr=2e-3, apply=True)
+    for _ in range(150):
+        last = d.trainStep(feat.data_ptr(), target.data_ptr(), n, h, w, lr=2e-3, apply=True)
+    assert _tc_error() == 0
+    assert last < 0.4 * first, (first, last)
+    d.close()
+
+
+def test_params_roundtrip(renderer, tmp_path):
+    d = api.Denoiser(renderer, seed=1)
+    p = d.getParams()
+    assert p.size == sum(9 * ci * co + co for ci, co, _ in LAYERS)
+    d.save(tmp_path / "w.bin")
+    e = api.Denoiser(renderer, seed=2)
+    assert not np.array_equal(e.getParams(), p)
+    e.load(tmp_path / "w.bin")
+    assert np.array_equal(e.getParams(), p)
+    with pytest.raises(N.KfError):
+        e.setParams(p[:-1])
+    d.close()
+    e.close()
+
+
+def _relmse(a, b):
+    x = np.asarray(a, np.float64).reshape(-1, 4)[:, :3]
+    y = np.asarray(b, np.float64).reshape(-1, 4)[:, :3]
+    return float(((x - y) ** 2 / (y ** 2 + 1e-2)).mean())
+
+
+def test_denoiser_beats_noisy_input_on_cornell():
+    """Train on Cornell variations (4 spp inputs, 256 spp targets), then denoise a held-out
+    variation: the denoised frame is closer to its 1024-spp reference than the 4-spp input."""
+    size = 64
+    cfg = scenes.cornell_config(spp=4, depth=5)
+    with api.Kuafu(cfg) as r:
+        d = api.Denoiser(r, seed=0)
+        for v in range(12):
+            s = r.createScene()
+            cam = scenes.cornell(r, size, size, scene=s, variation=100 + v)
+            d.addView(s, cam, 4, 64, 4)
+        assert d.numViews() == 12
+        d.train(300, batch=8, crop=48, lr=2e-3)
+        assert _tc_error() == 0
+        s = r.createScene()
+        cam = scenes.cornell(r, size, size, scene=s, variation=7)
+        r.setScene(s)
+        cfg.setPerPixelSampleRate(64)
+        r.applyConfig()
+        for _ in range(16):
+            r.run()
+        ref = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32).copy()   # running mean of 16 x 64 spp
+        cfg.setPerPixelSampleRate(4)
+        cfg.setAccumulatingFrames(False)
+        r.applyConfig()
+        r.run()
+        noisy = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32).copy()
+        d.apply(cam)
+        den = r.downloadAov(cam, N.KF_AOV_DENOISED_F32)
+        e_noisy, e_den = _relmse(noisy, ref), _relmse(den, ref)
+        print(f"relMSE 4 spp {e_noisy:.4e}, denoised {e_den:.4e}")
+        assert e_den < 0.5 * e_noisy
+        # the presented frame is the denoised one when use_denoiser is set
+        cfg.setUseDenoiser(True)
+        r.applyConfig()
+        with pytest.raises(N.KfError):
+            r.run()  # no denoiser attached
+        r.setDenoiser(d)
+        r.run()
+        den2 = r.downloadAov(cam, N.KF_AOV_DENOISED_F32)
+        frame = r.downloadLatestFrame(cam)
+        assert frame.shape == (size, size, 4)
+        r.setDenoiser(None)
+        d.close()
+        assert np.isfinite(den2).all()
