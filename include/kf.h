@@ -146,6 +146,10 @@ typedef struct kf_stats {
 } kf_stats;
 KF_API int kf_renderer_get_stats(kf_renderer r, kf_stats* out);
 KF_API int kf_renderer_reset_stats(kf_renderer r);
+/* Restart accumulation: the next run() stores its frame instead of blending it
+ * (kuafu sets global::frameCount = -1 only when the camera moves, camera.cpp:41-51,
+ * or the scene changes; this exposes the same reset directly). */
+KF_API int kf_renderer_reset_frame(kf_renderer r);
 /* Re-trace the last frame's traversal with per-ray counters (node / triangle /
  * instance visits) to give algorithmic bytes per ray. */
 KF_API int kf_renderer_count_traversal(kf_renderer r, int enable);
@@ -291,14 +295,18 @@ KF_API int kf_denoiser_apply(kf_denoiser d, kf_camera c);
  * use_denoiser is set: the presented frame (kf_renderer_download_latest_frame) is then
  * the denoised radiance; the accumulation target itself is left untouched. */
 KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d);
-/* Tensor-level entry points (device pointers, stream = the renderer's):
- * feat [n][h][w][32] BF16 network input, out [n][h][w][32] BF16 (channels 0..2 =
- * log1p radiance), target [n][h][w] float4 linear radiance; h, w % 16 == 0.
- * train_step computes loss and gradients (copied to grads_dev, may be NULL, FP32,
- * num_params) and, if apply, one Adam step with learning rate lr. */
-KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, int n, int h, int w, void* out);
-KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* target, int n, int h, int w,
-                                  float lr, float* grads_dev, int apply, float* loss);
+/* Tensor-level entry points (device pointers, stream = the renderer's). The network
+ * works on g(x) = asinh(x / 0.1) of linear radiance x.
+ * feat [n][h][w][32] BF16 network input (channels 0..2 g(noisy radiance), 3..5 albedo,
+ * 6..8 normal, 9 t / (1 + t), 10 log2(samples) / 8, rest 0); base [n][h][w] float4 FP32
+ * residual added to the network output (NULL = none; the renderer passes g(noisy));
+ * out [n][h][w][4] FP32 prediction in g space (channel 3 = 0); target [n][h][w] float4
+ * linear radiance; h, w % 16 == 0. train_step computes the L1 + gradient loss in g space
+ * and its gradients (copied to grads_dev, may be NULL, FP32, num_params) and, if apply,
+ * one Adam step with learning rate lr. */
+KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* base, int n, int h, int w, float* out);
+KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* base, const float* target, int n,
+                                  int h, int w, float lr, float* grads_dev, int apply, float* loss);
 
 /* ---- FP64 relative-MSE reduction: mean over pixels and channels of
  * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64 ---- */

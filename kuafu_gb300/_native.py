@@ -158,6 +158,7 @@ PROTOTYPES = {
     "kf_renderer_download_aov": (I, [VP, VP, I, VP, C.c_size_t]),
     "kf_renderer_get_stats": (I, [VP, C.POINTER(kf_stats)]),
     "kf_renderer_reset_stats": (I, [VP]),
+    "kf_renderer_reset_frame": (I, [VP]),
     "kf_renderer_count_traversal": (I, [VP, I]),
     "kf_material_init": (None, [C.POINTER(kf_material)]),
     "kf_material_add": (I, [C.POINTER(kf_material), C.POINTER(U32)]),
@@ -228,8 +229,8 @@ PROTOTYPES = {
     "kf_denoiser_train": (I, [VP, U32, U32, U32, F, C.POINTER(F)]),
     "kf_denoiser_apply": (I, [VP, VP]),
     "kf_renderer_set_denoiser": (I, [VP, VP]),
-    "kf_denoiser_forward": (I, [VP, VP, I, I, I, VP]),
-    "kf_denoiser_train_step": (I, [VP, VP, VP, I, I, I, F, VP, I, C.POINTER(F)]),
+    "kf_denoiser_forward": (I, [VP, VP, VP, I, I, I, VP]),
+    "kf_denoiser_train_step": (I, [VP, VP, VP, VP, I, I, I, F, VP, I, C.POINTER(F)]),
 }
 
 KF_AOV_RADIANCE_F32, KF_AOV_ALBEDO_F32, KF_AOV_NORMAL_F32, KF_AOV_DEPTH_F32 = 0, 1, 2, 3

@@ -464,6 +464,10 @@ class Kuafu:
         N.check(_lib().kf_renderer_get_stats(self._h, C.byref(s)))
         return s
 
+    def resetFrame(self):
+        """Restart accumulation (the next run() stores instead of blending)."""
+        N.check(_lib().kf_renderer_reset_frame(self._h))
+
     def resetStats(self):
         N.check(_lib().kf_renderer_reset_stats(self._h))
 
@@ -542,14 +546,14 @@ class Denoiser:
     def apply(self, cam: Camera):
         N.check(_lib().kf_denoiser_apply(self._h, cam._h))
 
-    def forward(self, feat_ptr: int, n: int, h: int, w: int, out_ptr: int):
-        N.check(_lib().kf_denoiser_forward(self._h, feat_ptr, n, h, w, out_ptr))
+    def forward(self, feat_ptr: int, n: int, h: int, w: int, out_ptr: int, base_ptr: int | None = None):
+        N.check(_lib().kf_denoiser_forward(self._h, feat_ptr, base_ptr, n, h, w, out_ptr))
 
     def trainStep(self, feat_ptr: int, target_ptr: int, n: int, h: int, w: int, lr: float = 0.0,
-                  grads_ptr: int | None = None, apply: bool = False) -> float:
+                  grads_ptr: int | None = None, apply: bool = False, base_ptr: int | None = None) -> float:
         loss = C.c_float()
-        N.check(_lib().kf_denoiser_train_step(self._h, feat_ptr, target_ptr, n, h, w, float(lr), grads_ptr,
-                                              int(bool(apply)), C.byref(loss)))
+        N.check(_lib().kf_denoiser_train_step(self._h, feat_ptr, base_ptr, target_ptr, n, h, w, float(lr),
+                                              grads_ptr, int(bool(apply)), C.byref(loss)))
         return loss.value
 
 

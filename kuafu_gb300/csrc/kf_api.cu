@@ -438,6 +438,12 @@ KF_API int kf_renderer_get_stats(kf_renderer r, kf_stats* out) {
         *out = r->stats;
     });
 }
+KF_API int kf_renderer_reset_frame(kf_renderer r) {
+    return guarded([&] {
+        REQ(r, "invalid renderer");
+        frame_reset(r);
+    });
+}
 KF_API int kf_renderer_reset_stats(kf_renderer r) {
     return guarded([&] {
         REQ(r, "invalid renderer");
@@ -1175,20 +1181,20 @@ KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d) {
         r->denoiser = d;
     });
 }
-KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, int n, int h, int w, void* out) {
+KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* base, int n, int h, int w, float* out) {
     return guarded([&] {
         REQ(feat && out && n > 0 && h > 0 && w > 0, "invalid tensor");
         check_denoiser(d);
-        denoiser_forward(d, feat, n, h, w, out);
+        denoiser_forward(d, feat, base, n, h, w, out);
         sync_stream(denoiser_renderer(d));
     });
 }
-KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* target, int n, int h, int w,
-                                  float lr, float* grads_dev, int apply, float* loss) {
+KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* base, const float* target, int n,
+                                  int h, int w, float lr, float* grads_dev, int apply, float* loss) {
     return guarded([&] {
         REQ(feat && target && n > 0 && h > 0 && w > 0, "invalid tensor");
         check_denoiser(d);
-        const float l = denoiser_train_step(d, feat, target, n, h, w, lr, grads_dev, apply != 0);
+        const float l = denoiser_train_step(d, feat, base, target, n, h, w, lr, grads_dev, apply != 0);
         if (loss) *loss = l;
     });
 }

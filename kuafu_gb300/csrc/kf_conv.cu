@@ -46,7 +46,7 @@ struct TcParams {
     int relu;
     __nv_bfloat16* out;
     int out_cstride, out_coff;
-    float* outf;      // gemm output (atomic add)
+    float* outf;      // gemm output (atomic add); conv: FP32 output instead of BF16 when set
     int ldo, M_valid, N_valid;
     int k_iters, k_per_split;
     uint32_t tmem_cols;
@@ -166,8 +166,7 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
     if (MODE == 0) {
         const int px = x0 + (row % p.bw), py = y0 + (row / p.bw);
         const bool valid = ready && nk > 0 && px < p.W && py < p.H;
-        __nv_bfloat16* dst =
-            p.out + ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
+        const size_t base = ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
         for (int c = 0; c < p.n_tile; c += 8) {
             uint32_t r[8];
             tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
@@ -181,6 +180,11 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
                 if (p.bias && co + j < p.Cout) v[j] += p.bias[co + j];
                 if (p.relu) v[j] = fmaxf(v[j], 0.0f);
             }
+            if (p.outf) { // FP32 output (a network head)
+                for (int j = 0; j < 8 && co + j < p.Cout; ++j) p.outf[base + co + j] = v[j];
+                continue;
+            }
+            __nv_bfloat16* dst = p.out + base;
             if (co + 8 <= p.Cout && ((p.out_coff + co) & 7) == 0 && (p.out_cstride & 7) == 0) {
                 __nv_bfloat162 q[4];
 #pragma unroll
@@ -275,8 +279,9 @@ template <int MODE, int SWZ> void launch_tc(dim3 grid, const CUtensorMap& a, con
 
 void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
                   const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
-                  cudaStream_t st) {
+                  cudaStream_t st, float* y_f32) {
     KF_REQUIRE(N > 0 && H > 0 && W > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: empty tensor");
+    KF_REQUIRE(y || y_f32, KF_ERR_INVALID_ARGUMENT, "conv3x3: no output tensor");
     KF_REQUIRE(Cin % 32 == 0 && Cin > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: input channels must be a multiple of 32");
     KF_REQUIRE(Cout > 0 && Cout <= Cout_rows && Cout_rows % 16 == 0, KF_ERR_INVALID_ARGUMENT,
                "conv3x3: weight rows must be a multiple of 16 covering the output channels");
@@ -307,6 +312,7 @@ void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     p.bias = bias;
     p.relu = relu ? 1 : 0;
     p.out = y;
+    p.outf = y_f32;
     p.out_cstride = y_cstride;
     p.out_coff = y_coff;
     p.tmem_cols = pow2_at_least((uint32_t)n_tile);

@@ -190,12 +190,19 @@ __global__ void k_pack_layer(const float* __restrict__ W, int cin, int cout, int
     }
 }
 
-// Network input from render targets: log1p(radiance), albedo (base colour of the first hit
-// of sample 0), normal, hit distance t / (1 + t); 32 channels, the rest zero. Pixels of the
-// padded tensor outside (H, W) are zero.
+// The network works on g(x) = asinh(x / kTone) of linear radiance: g'(x) = 1 / sqrt(x^2 +
+// kTone^2), so errors in g space weigh like the relMSE metric (x - ref)^2 / (ref^2 + 1e-2).
+constexpr float kTone = 0.1f;
+__device__ __forceinline__ float tone(float x) { return asinhf(fmaxf(x, 0.0f) * (1.0f / kTone)); }
+__device__ __forceinline__ float untone(float y) { return kTone * sinhf(fmaxf(y, 0.0f)); }
+
+// Network input from render targets: g(radiance), albedo (base colour of the first hit of
+// sample 0), normal, hit distance t / (1 + t), log2(samples) / 8; 32 channels, the rest
+// zero. base (optional) receives g(radiance) in FP32: the residual the network corrects.
+// Pixels of the padded tensor outside (H, W) are zero.
 __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __restrict__ alb,
-                                const float4* __restrict__ nrm, const float* __restrict__ dep, int H, int W, int Hp,
-                                int Wp, bf16* out) {
+                                const float4* __restrict__ nrm, const float* __restrict__ dep, float spp_feature,
+                                int H, int W, int Hp, int Wp, bf16* out, float4* base) {
     const size_t total = (size_t)Hp * Wp;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % Wp), y = (int)(i / Wp);
@@ -205,9 +212,9 @@ __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __
             const size_t s = (size_t)y * W + x;
             const float4 r = rad[s], a = alb[s], n = nrm[s];
             const float d = dep[s];
-            f[0] = log1pf(fmaxf(r.x, 0.0f));
-            f[1] = log1pf(fmaxf(r.y, 0.0f));
-            f[2] = log1pf(fmaxf(r.z, 0.0f));
+            f[0] = tone(r.x);
+            f[1] = tone(r.y);
+            f[2] = tone(r.z);
             f[3] = a.x;
             f[4] = a.y;
             f[5] = a.z;
@@ -215,25 +222,39 @@ __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __
             f[7] = n.y;
             f[8] = n.z;
             f[9] = d / (1.0f + d);
+            f[10] = spp_feature;
         }
         bf16* o = out + i * 32;
         for (int c = 0; c < 32; ++c) o[c] = __float2bfloat16_rn(f[c]);
+        if (base) base[i] = make_float4(f[0], f[1], f[2], 0.0f);
     }
 }
 
-// denoised linear radiance = expm1(prediction) for the (H, W) window of the padded output
-__global__ void k_unpack(const bf16* __restrict__ pred, int H, int W, int Wp, float4* out) {
+// head[p].xyz += base[p].xyz (the residual connection around the network)
+__global__ void k_add_base(float4* __restrict__ head, const float4* __restrict__ base, size_t P) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 b = base[i];
+        float4 h = head[i];
+        h.x += b.x;
+        h.y += b.y;
+        h.z += b.z;
+        head[i] = h;
+    }
+}
+
+// denoised linear radiance = g^-1(prediction) for the (H, W) window of the padded output
+__global__ void k_unpack(const float4* __restrict__ pred, int H, int W, int Wp, float4* out) {
     const size_t total = (size_t)H * W;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % W), y = (int)(i / W);
-        const bf16* p = pred + ((size_t)y * Wp + x) * 32;
-        out[i] = make_float4(expm1f(fmaxf(__bfloat162float(p[0]), 0.0f)), expm1f(fmaxf(__bfloat162float(p[1]), 0.0f)),
-                             expm1f(fmaxf(__bfloat162float(p[2]), 0.0f)), 1.0f);
+        const float4 p = pred[(size_t)y * Wp + x];
+        out[i] = make_float4(untone(p.x), untone(p.y), untone(p.z), 1.0f);
     }
 }
 
-// L = mean|p - t| + lambda * mean(|dx p - dx t| + |dy p - dy t|) in log1p space; writes dL/dp.
-__global__ void k_loss(const bf16* __restrict__ pred, const float4* __restrict__ target, int N, int H, int W,
+// L = mean|p - t| + lambda * mean(|dx p - dx t| + |dy p - dy t|) in g space, p the FP32
+// prediction [P][4], t = g(target); writes dL/dp as the BF16 [P][32] gradient of the head.
+__global__ void k_loss(const float* __restrict__ pred, const float4* __restrict__ target, int N, int H, int W,
                        float lambda, float* loss, bf16* gpred) {
     const size_t total = (size_t)N * H * W;
     const float inv = 1.0f / (float)(total * 3);
@@ -242,14 +263,13 @@ __global__ void k_loss(const bf16* __restrict__ pred, const float4* __restrict__
         const int x = (int)(i % W);
         const int y = (int)((i / W) % H);
         const float4 t4 = target[i];
-        const float tv[3] = {log1pf(fmaxf(t4.x, 0.0f)), log1pf(fmaxf(t4.y, 0.0f)), log1pf(fmaxf(t4.z, 0.0f))};
+        const float tv[3] = {tone(t4.x), tone(t4.y), tone(t4.z)};
         bf16* g = gpred + i * 32;
         for (int c = 0; c < 3; ++c) {
-            auto P = [&](size_t j) { return __bfloat162float(pred[j * 32 + c]); };
+            auto P = [&](size_t j) { return pred[j * 4 + c]; };
             auto T = [&](size_t j) {
                 const float4 q = target[j];
-                const float v = c == 0 ? q.x : (c == 1 ? q.y : q.z);
-                return log1pf(fmaxf(v, 0.0f));
+                return tone(c == 0 ? q.x : (c == 1 ? q.y : q.z));
             };
             const float p = P(i);
             float d = p - tv[c];
@@ -282,9 +302,10 @@ __global__ void k_loss(const bf16* __restrict__ pred, const float4* __restrict__
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc * inv);
 }
 
-// crop gather: features [n][H][W][32] and targets -> batch [b][c][c]
-__global__ void k_gather_crops(const bf16* __restrict__ feat, const float4* __restrict__ tgt, int H, int W,
-                               const int4* __restrict__ crops, int B, int c, bf16* bf, float4* bt) {
+// crop gather: features [n][H][W][32], residual bases and targets -> batch [b][c][c]
+__global__ void k_gather_crops(const bf16* __restrict__ feat, const float4* __restrict__ base,
+                               const float4* __restrict__ tgt, int H, int W, const int4* __restrict__ crops, int B,
+                               int c, bf16* bf, float4* bb, float4* bt) {
     const size_t total = (size_t)B * c * c;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % c);
@@ -295,6 +316,7 @@ __global__ void k_gather_crops(const bf16* __restrict__ feat, const float4* __re
         const uint4* s = reinterpret_cast<const uint4*>(feat + src * 32);
         uint4* d = reinterpret_cast<uint4*>(bf + i * 32);
         for (int k = 0; k < 4; ++k) d[k] = s[k];
+        bb[i] = base[src];
         bt[i] = tgt[src];
     }
 }
@@ -323,6 +345,7 @@ struct Layer {
 struct Acts {
     int n = 0, h = 0, w = 0;
     DeviceBuffer<bf16> buf; // one arena for every activation and activation gradient
+    DeviceBuffer<float> head; // FP32 network output [P][4] (log1p radiance, 0)
     std::vector<size_t> off;
     bf16* at(int k) { return buf.ptr + off[k]; }
 };
@@ -353,9 +376,10 @@ struct kf_denoiser_s {
     // dataset
     int ds_h = 0, ds_w = 0, ds_n = 0;
     kf::DeviceBuffer<__nv_bfloat16> ds_feat;
-    kf::DeviceBuffer<float4> ds_tgt;
+    kf::DeviceBuffer<float4> ds_base, ds_tgt;
     kf::DeviceBuffer<__nv_bfloat16> batch_feat;
-    kf::DeviceBuffer<float4> batch_tgt;
+    kf::DeviceBuffer<float4> batch_base, batch_tgt;
+    kf::DeviceBuffer<float4> apply_base; // residual base of an inference frame
     kf::DeviceBuffer<int4> crops;
     std::mt19937 rng{1234};
 };
@@ -470,6 +494,8 @@ void ensure_acts(kf_denoiser_impl& d, int n, int h, int w, cudaStream_t st) {
     total += (zt_max + 127) / 128 * 128;
     a.buf.resize(total, st);
     KF_CUDA_CHECK(cudaMemsetAsync(a.buf.ptr, 0, a.buf.bytes(), st));
+    a.head.resize(P0 * 4, st);
+    KF_CUDA_CHECK(cudaMemsetAsync(a.head.ptr, 0, a.head.bytes(), st));
     a.n = n;
     a.h = h;
     a.w = w;
@@ -533,7 +559,8 @@ void up_fwd(Ctx& c, TRef x, int level_hi, TRef y) {
     k_up_fwd<<<grid_for(n), 256, 0, c.st>>>(x.p, x.c, c.n, c.H(level_hi), c.W(level_hi), y.p, y.cs, y.co);
 }
 
-void forward(Ctx& c) {
+// prediction (in a.head) = network(T_IN) + base (FP32 residual, optional)
+void forward(Ctx& c, const float4* base) {
     Acts& a = c.d.acts;
     conv_fwd(c, 0, 0, T(a, T_IN), T(a, T_E0A));
     conv_fwd(c, 1, 0, T(a, T_E0A), S(a, T_CAT0, 64, 32));
@@ -561,7 +588,13 @@ void forward(Ctx& c) {
     up_fwd(c, T(a, T_D1B), 0, S(a, T_CAT0, 0, 64));
     conv_fwd(c, 16, 0, T(a, T_CAT0), T(a, T_D0A));
     conv_fwd(c, 17, 0, T(a, T_D0A), T(a, T_D0B));
-    conv_fwd(c, 18, 0, T(a, T_D0B), TRef{a.at(T_OUT), 32, 0, 3});
+    {
+        const Layer& l = c.d.L[18];
+        conv3x3_bf16(a.at(T_D0B), c.n, c.h, c.w, 32, c.d.wf.ptr + l.wf_off, l.rows, c.d.params.ptr + l.b_off, l.cout,
+                     false, nullptr, 4, 0, c.st, a.head.ptr);
+    }
+    if (base)
+        k_add_base<<<grid_for(c.P(0)), 256, 0, c.st>>>(reinterpret_cast<float4*>(a.head.ptr), base, c.P(0));
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -641,26 +674,27 @@ void denoiser_set_params(kf_denoiser_impl* d, const float* in, size_t n) {
     d->step = 0;
 }
 
-// out: [n, h, w, 32] BF16 device buffer (channels 0..2 = prediction in log1p space)
-void denoiser_forward(kf_denoiser_impl* d, const void* feat, int n, int h, int w, void* out) {
+// out: [n, h, w, 4] FP32 device buffer (channels 0..2 = prediction in g space, 3 = 0);
+// base: optional FP32 residual [n, h, w] float4 added to the network output.
+void denoiser_forward(kf_denoiser_impl* d, const void* feat, const void* base, int n, int h, int w, void* out) {
     cudaStream_t st = d->r->stream;
     ensure_acts(*d, n, h, w, st);
     if (!d->packed) pack(*d, st);
     KF_CUDA_CHECK(cudaMemcpyAsync(d->acts.at(T_IN), feat, (size_t)n * h * w * 32 * 2, cudaMemcpyDeviceToDevice, st));
     Ctx c{*d, st, n, h, w};
-    forward(c);
+    forward(c, static_cast<const float4*>(base));
     if (out)
-        KF_CUDA_CHECK(cudaMemcpyAsync(out, d->acts.at(T_OUT), (size_t)n * h * w * 32 * 2, cudaMemcpyDeviceToDevice, st));
+        KF_CUDA_CHECK(cudaMemcpyAsync(out, d->acts.head.ptr, (size_t)n * h * w * 16, cudaMemcpyDeviceToDevice, st));
 }
 
-float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const float* tgt, int n, int h, int w, float lr,
-                          float* grads_out, bool apply_update) {
+float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const void* base, const float* tgt, int n, int h,
+                          int w, float lr, float* grads_out, bool apply_update) {
     cudaStream_t st = d->r->stream;
-    denoiser_forward(d, feat, n, h, w, nullptr);
+    denoiser_forward(d, feat, base, n, h, w, nullptr);
     Acts& a = d->acts;
     KF_CUDA_CHECK(cudaMemsetAsync(d->loss.ptr, 0, sizeof(float), st));
     const size_t P = (size_t)n * h * w;
-    k_loss<<<grid_for(P), 256, 0, st>>>(a.at(T_OUT), reinterpret_cast<const float4*>(tgt), n, h, w, 0.5f, d->loss.ptr,
+    k_loss<<<grid_for(P), 256, 0, st>>>(a.head.ptr, reinterpret_cast<const float4*>(tgt), n, h, w, 0.5f, d->loss.ptr,
                                         a.at(G_OUT));
     KF_CUDA_CHECK(cudaMemsetAsync(d->grads.ptr, 0, d->grads.bytes(), st));
     Ctx c{*d, st, n, h, w};
@@ -681,12 +715,36 @@ float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const float* tg
     return loss;
 }
 
-// Features of a camera's current render targets into a padded [1][Hp][Wp][32] tensor.
-static void camera_features(kf_camera_s* c, bf16* out, int Hp, int Wp, cudaStream_t st) {
+// Features (and residual base) of a camera's current render targets, padded to [1][Hp][Wp].
+static void camera_features(kf_camera_s* c, uint32_t samples, bf16* out, float4* base, int Hp, int Wp,
+                            cudaStream_t st) {
+    const float spp_feature = std::log2((float)std::max(samples, 1u)) / 8.0f;
     k_pack_features<<<grid_for((size_t)Hp * Wp), 256, 0, st>>>(c->accum.ptr, c->albedo.ptr, c->normal.ptr,
-                                                               c->depth.ptr, c->target_h, c->target_w, Hp, Wp, out);
+                                                               c->depth.ptr, spp_feature, c->target_h, c->target_w,
+                                                               Hp, Wp, out, base);
     KF_CUDA_CHECK(cudaGetLastError());
 }
+
+namespace {
+// kuafu's frame state, restored when a training render leaves its scope
+struct FrameStateGuard {
+    kf_renderer_s* r;
+    uint32_t accumulate;
+    explicit FrameStateGuard(kf_renderer_s* rr) : r(rr), accumulate(rr->cfg.accumulate_frames) {}
+    ~FrameStateGuard() {
+        r->frame_count = -1;
+        r->cfg.accumulate_frames = accumulate;
+    }
+};
+
+template <class T> void grow(DeviceBuffer<T>& b, size_t old_n, size_t new_n, cudaStream_t st) {
+    DeviceBuffer<T> nb;
+    nb.resize(new_n, st);
+    if (old_n) KF_CUDA_CHECK(cudaMemcpyAsync(nb.ptr, b.ptr, old_n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    KF_CUDA_CHECK(cudaStreamSynchronize(st));
+    b = std::move(nb);
+}
+} // namespace
 
 void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint32_t low_spp, uint32_t high_spp,
                        uint32_t high_frames) {
@@ -701,33 +759,21 @@ void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint3
     KF_REQUIRE(c->width == d->ds_w && c->height == d->ds_h, KF_ERR_INVALID_ARGUMENT,
                "all training views must have the same size");
     const size_t npix = (size_t)c->width * c->height;
-    // grow the dataset (copying the existing examples)
-    {
-        DeviceBuffer<bf16> nf;
-        DeviceBuffer<float4> nt;
-        nf.resize(npix * 32 * (d->ds_n + 1), st);
-        nt.resize(npix * (d->ds_n + 1), st);
-        if (d->ds_n) {
-            KF_CUDA_CHECK(cudaMemcpyAsync(nf.ptr, d->ds_feat.ptr, npix * 32 * 2 * d->ds_n, cudaMemcpyDeviceToDevice, st));
-            KF_CUDA_CHECK(cudaMemcpyAsync(nt.ptr, d->ds_tgt.ptr, npix * 16 * d->ds_n, cudaMemcpyDeviceToDevice, st));
-        }
-        KF_CUDA_CHECK(cudaStreamSynchronize(st));
-        d->ds_feat = std::move(nf);
-        d->ds_tgt = std::move(nt);
-    }
-    const uint32_t accumulate = r->cfg.accumulate_frames;
+    const size_t k = (size_t)d->ds_n;
+    grow(d->ds_feat, npix * 32 * k, npix * 32 * (k + 1), st);
+    grow(d->ds_base, npix * k, npix * (k + 1), st);
+    grow(d->ds_tgt, npix * k, npix * (k + 1), st);
+    FrameStateGuard guard(r);
     r->cfg.accumulate_frames = 1;
     // noisy input: one frame of low_spp samples
     r->frame_count = -1;
     render_frame(r, s, c, low_spp);
-    camera_features(c, d->ds_feat.ptr + npix * 32 * d->ds_n, c->height, c->width, st);
-    // target: high_frames frames of high_spp samples, running mean
+    camera_features(c, low_spp, d->ds_feat.ptr + npix * 32 * k, d->ds_base.ptr + npix * k, c->height, c->width, st);
+    // target: running mean of high_frames frames of high_spp samples
     r->frame_count = -1;
     for (uint32_t f = 0; f < high_frames; ++f) render_frame(r, s, c, high_spp);
-    KF_CUDA_CHECK(cudaMemcpyAsync(d->ds_tgt.ptr + npix * d->ds_n, c->accum.ptr, npix * 16, cudaMemcpyDeviceToDevice, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(d->ds_tgt.ptr + npix * k, c->accum.ptr, npix * 16, cudaMemcpyDeviceToDevice, st));
     KF_CUDA_CHECK(cudaStreamSynchronize(st));
-    r->frame_count = -1;
-    r->cfg.accumulate_frames = accumulate;
     ++d->ds_n;
 }
 
@@ -738,6 +784,7 @@ float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32
     cudaStream_t st = d->r->stream;
     const size_t per = (size_t)crop * crop;
     d->batch_feat.resize(per * 32 * batch, st);
+    d->batch_base.resize(per * batch, st);
     d->batch_tgt.resize(per * batch, st);
     d->crops.resize(batch, st);
     std::vector<int4> cr(batch);
@@ -750,27 +797,33 @@ float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32
             cr[b].w = 0;
         }
         d->crops.upload(cr.data(), batch, st);
-        k_gather_crops<<<grid_for(per * batch), 256, 0, st>>>(d->ds_feat.ptr, d->ds_tgt.ptr, d->ds_h, d->ds_w,
-                                                              d->crops.ptr, (int)batch, (int)crop, d->batch_feat.ptr,
-                                                              d->batch_tgt.ptr);
-        acc += denoiser_train_step(d, d->batch_feat.ptr, reinterpret_cast<const float*>(d->batch_tgt.ptr), (int)batch,
-                                   (int)crop, (int)crop, lr, nullptr, true);
+        k_gather_crops<<<grid_for(per * batch), 256, 0, st>>>(d->ds_feat.ptr, d->ds_base.ptr, d->ds_tgt.ptr, d->ds_h,
+                                                              d->ds_w, d->crops.ptr, (int)batch, (int)crop,
+                                                              d->batch_feat.ptr, d->batch_base.ptr, d->batch_tgt.ptr);
+        acc += denoiser_train_step(d, d->batch_feat.ptr, d->batch_base.ptr,
+                                   reinterpret_cast<const float*>(d->batch_tgt.ptr), (int)batch, (int)crop, (int)crop,
+                                   lr, nullptr, true);
     }
     return iters ? (float)(acc / iters) : 0.0f;
 }
 
 void denoiser_apply(kf_denoiser_impl* d, kf_camera_s* c) {
-    cudaStream_t st = d->r->stream;
+    kf_renderer_s* r = d->r;
+    cudaStream_t st = r->stream;
     KF_REQUIRE(c->has_frame, KF_ERR_STATE, "the camera has no frame to denoise");
     const int Hp = (c->target_h + 15) / 16 * 16, Wp = (c->target_w + 15) / 16 * 16;
     ensure_acts(*d, 1, Hp, Wp, st);
     if (!d->packed) pack(*d, st);
-    camera_features(c, d->acts.at(T_IN), Hp, Wp, st);
+    const size_t P = (size_t)Hp * Wp;
+    if (d->apply_base.count < P) d->apply_base.resize(P, st);
+    const uint32_t frames = (r->cfg.accumulate_frames && r->frame_count >= 0) ? (uint32_t)r->frame_count + 1u : 1u;
+    camera_features(c, frames * std::max(r->stats.last_spp, 1u), d->acts.at(T_IN), d->apply_base.ptr, Hp, Wp, st);
     Ctx cx{*d, st, 1, Hp, Wp};
-    forward(cx);
+    forward(cx, d->apply_base.ptr);
     const size_t npix = (size_t)c->target_w * c->target_h;
     if (c->denoised.count != npix) c->denoised.resize(npix, st);
-    k_unpack<<<grid_for(npix), 256, 0, st>>>(d->acts.at(T_OUT), c->target_h, c->target_w, Wp, c->denoised.ptr);
+    k_unpack<<<grid_for(npix), 256, 0, st>>>(reinterpret_cast<const float4*>(d->acts.head.ptr), c->target_h,
+                                             c->target_w, Wp, c->denoised.ptr);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 

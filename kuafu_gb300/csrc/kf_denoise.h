@@ -21,11 +21,12 @@ kf_renderer_s* denoiser_renderer(const kf_denoiser_impl* d);
 void denoiser_get_params(kf_denoiser_impl* d, float* out, size_t n);
 void denoiser_set_params(kf_denoiser_impl* d, const float* in, size_t n);
 
-// Tensor-level entry points (device pointers): feat [n][h][w][32] BF16, out [n][h][w][32] BF16,
+// Tensor-level entry points (device pointers): feat [n][h][w][32] BF16, out [n][h][w][4] FP32,
 // tgt [n][h][w] float4 linear radiance. h and w divisible by 16.
-void denoiser_forward(kf_denoiser_impl* d, const void* feat, int n, int h, int w, void* out);
-float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const float* tgt, int n, int h, int w, float lr,
-                          float* grads_out, bool apply_update);
+// base (optional): FP32 [n][h][w] float4 residual added to the network output.
+void denoiser_forward(kf_denoiser_impl* d, const void* feat, const void* base, int n, int h, int w, void* out);
+float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const void* base, const float* tgt, int n, int h,
+                          int w, float lr, float* grads_out, bool apply_update);
 
 // Renders one training pair of a camera: a low_spp frame (input) and high_frames x high_spp (target).
 void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint32_t low_spp, uint32_t high_spp,

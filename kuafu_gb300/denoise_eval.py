@@ -1,0 +1,263 @@
+"""Time-to-relMSE of the learned denoiser against plain accumulation.
+
+The scene is the Cornell box (256-spp-class workload of kuafu's example, built
+procedurally) rendered at 1920x1080, path depth 5, no Russian roulette. The
+experiment, all on one GPU:
+
+1. Reference: two independent FP64 accumulations (seeds A and B) of ref_spp / 2
+   samples each; ref = their mean. relMSE(A, B) / 4 estimates the reference's own
+   noise floor (the expected relMSE of a noise-free image against this reference),
+   reported as `ref_floor`. "Debiased" relMSE values subtract that floor.
+2. Plain accumulation (an independent seed): frames of `plain_frame_spp` samples,
+   relMSE after each checkpoint, cumulative GPU time from CUDA events.
+3. Learned denoiser: trained on this renderer's own pairs (Cornell variations at
+   256x256, inputs at 1..64 spp, targets at high spp), then applied to single
+   frames of k spp of the held-out scene; time = render + denoise (CUDA events).
+4. For each threshold tau: the time plain accumulation needs to reach relMSE <= tau
+   (measured, or extrapolated from its c / N fit past the last checkpoint, flagged)
+   and the time the denoised form needs (smallest k whose denoised frame reaches
+   tau, or None).
+
+relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2), reduced
+in FP64 on the GPU (kf_relmse).
+
+  python -m kuafu_gb300.denoise_eval [--small] [--json out.json]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+from . import _native as N
+from . import api, scenes
+
+EPS = 1e-2
+
+# (cin, cout) of the U-Net convolutions (kf_denoise.cu) and their resolution level
+_LAYERS = [(32, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 96, 2), (96, 96, 2), (96, 128, 3),
+           (128, 128, 3), (128, 160, 4), (160, 160, 4), (288, 128, 3), (128, 128, 3), (224, 96, 2), (96, 96, 2),
+           (160, 64, 1), (64, 64, 1), (96, 32, 0), (32, 32, 0), (32, 3, 0)]
+
+
+def unet_flops(h: int, w: int) -> float:
+    """Dense multiply-add FLOPs of one inference (2 * H_l * W_l * Cin * Cout * 9 summed over convs)."""
+    hp, wp = (h + 15) // 16 * 16, (w + 15) // 16 * 16
+    return float(sum(2.0 * (hp >> l) * (wp >> l) * ci * co * 9 for ci, co, l in _LAYERS))
+
+
+class _Timer:
+    """CUDA events on the renderer's stream."""
+
+    def __init__(self, r: api.Kuafu):
+        import torch
+
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(r.stream())
+
+    def __enter__(self):
+        t = self.torch
+        self.e0 = t.cuda.Event(enable_timing=True)
+        self.e1 = t.cuda.Event(enable_timing=True)
+        self.e0.record(self.stream)
+        return self
+
+    def __exit__(self, *a):
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        self.ms = self.e0.elapsed_time(self.e1)
+
+
+def _gpu_relmse(r: api.Kuafu, x: np.ndarray, ref: np.ndarray) -> float:
+    """kf_relmse over float4 images (host arrays uploaded to the device)."""
+    import ctypes as C
+
+    import torch
+
+    a = torch.from_numpy(np.ascontiguousarray(x, np.float32).reshape(-1, 4)).cuda()
+    b = torch.from_numpy(np.ascontiguousarray(ref, np.float32).reshape(-1, 4)).cuda()
+    torch.cuda.synchronize()
+    out = C.c_double()
+    N.check(N.load().kf_relmse(r._h, a.data_ptr(), b.data_ptr(), a.shape[0], EPS, C.byref(out)))
+    return out.value
+
+
+def _fp64_mean(r: api.Kuafu, cam: api.Camera) -> np.ndarray:
+    s = r.downloadAov(cam, N.KF_AOV_SUM_F64)
+    out = np.ones(s.shape, np.float64)
+    out[..., :3] = s[..., :3] / s[..., 3:4]
+    return out
+
+
+def _accumulate(r, cfg, cam, seed, spp_total, frame_spp):
+    cfg.setSeed(seed)
+    cfg.setPerPixelSampleRate(frame_spp)
+    cfg.setAccumulatingFrames(True)
+    cfg.setUseDenoiser(False)
+    r.applyConfig()
+    r.resetFrame()
+    for _ in range(spp_total // frame_spp):
+        r.run()
+    r.synchronize()
+    return _fp64_mean(r, cam)
+
+
+def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp=8, plain_max_spp=1024,
+        train_views=64, train_size=256, train_high_spp=64, train_high_frames=64, train_iters=3000,
+        train_batch=8, train_crop=128, lr=1e-3, denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256),
+        thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3), depth=5, log=print) -> dict:
+    cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
+    res = {"scene": "cornell", "width": width, "height": height, "depth": depth, "eps": EPS}
+    with api.Kuafu(cfg) as r:
+        scene = r.getScene()
+        cam = scenes.cornell(r, width, height, scene=scene)
+        # 1. reference halves
+        t0 = time.perf_counter()
+        a = _accumulate(r, cfg, cam, 1001, ref_spp // 2, ref_frame_spp)
+        b = _accumulate(r, cfg, cam, 1002, ref_spp // 2, ref_frame_spp)
+        ref = 0.5 * (a + b)
+        floor = _gpu_relmse(r, a, b) / 4.0
+        res["reference"] = {"spp": ref_spp, "accumulation": "fp64", "halves_relmse": 4.0 * floor,
+                            "ref_floor": floor, "seconds": time.perf_counter() - t0}
+        log(f"reference {ref_spp} spp: floor {floor:.4e} ({time.perf_counter() - t0:.1f} s)")
+
+        # 2. plain accumulation
+        timer = _Timer(r)
+        cfg.setSeed(7)
+        cfg.setPerPixelSampleRate(plain_frame_spp)
+        cfg.setAccumulatingFrames(True)
+        r.applyConfig()
+        r.resetFrame()
+        r.run()  # graph capture outside the timed frames
+        r.synchronize()
+        r.resetFrame()
+        plain = []
+        t_ms, spp = 0.0, 0
+        next_cp = plain_frame_spp
+        while spp < plain_max_spp:
+            with timer:
+                r.run()
+            t_ms += timer.ms
+            spp += plain_frame_spp
+            if spp >= next_cp:
+                img = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
+                e = _gpu_relmse(r, img, ref)
+                plain.append({"spp": spp, "ms": t_ms, "relmse": e, "relmse_debiased": e - floor})
+                next_cp *= 2
+        res["plain"] = plain
+        log("plain: " + ", ".join(f"{p['spp']}spp {p['relmse']:.3e}" for p in plain))
+        # c / N fit on the debiased values of the last half of the checkpoints
+        tail = [p for p in plain if p["spp"] >= plain[len(plain) // 2]["spp"]]
+        c_fit = float(np.median([max(p["relmse_debiased"], 0.0) * p["spp"] for p in tail]))
+        ms_per_spp = plain[-1]["ms"] / plain[-1]["spp"]
+        res["plain_fit"] = {"c": c_fit, "ms_per_spp": ms_per_spp}
+
+        # 3. denoiser training on Cornell variations
+        d = api.Denoiser(r, seed=0)
+        t0 = time.perf_counter()
+        for v in range(train_views):
+            s = r.createScene()
+            c = scenes.cornell(r, train_size, train_size, scene=s, variation=1000 + v)
+            cfg.setSeed(50000 + v)
+            r.applyConfig()
+            d.addView(s, c, denoise_spps[v % len(denoise_spps)], train_high_spp, train_high_frames)
+        t_data = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        losses = []
+        chunk = max(1, train_iters // 10)
+        done = 0
+        while done < train_iters:
+            k = min(chunk, train_iters - done)
+            cur_lr = lr * (0.1 if done >= 0.8 * train_iters else 1.0)
+            losses.append(d.train(k, train_batch, train_crop, cur_lr))
+            done += k
+        r.synchronize()
+        t_train = time.perf_counter() - t0
+        res["training"] = {"views": train_views, "size": train_size, "input_spp": list(denoise_spps),
+                           "target_spp": train_high_spp * train_high_frames, "iters": train_iters,
+                           "batch": train_batch, "crop": train_crop, "lr": lr, "loss_curve": losses,
+                           "data_seconds": t_data, "train_seconds": t_train}
+        log(f"training: data {t_data:.1f} s, {train_iters} iters {t_train:.1f} s, loss {losses[0]:.4f} -> "
+            f"{losses[-1]:.4f}")
+
+        # 4. denoised single frames of the held-out scene
+        r.setScene(scene)
+        den = []
+        flops = unet_flops(height, width)
+        for k in denoise_spps:
+            cfg.setSeed(9)
+            cfg.setPerPixelSampleRate(k)
+            cfg.setAccumulatingFrames(False)
+            r.applyConfig()
+            r.resetFrame()
+            r.run()  # capture
+            d.apply(cam)
+            r.synchronize()
+            with timer:
+                r.run()
+            t_render = timer.ms
+            noisy = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
+            with timer:
+                d.apply(cam)
+            t_dn = timer.ms
+            out = r.downloadAov(cam, N.KF_AOV_DENOISED_F32)
+            e_n = _gpu_relmse(r, noisy, ref)
+            e_d = _gpu_relmse(r, out, ref)
+            den.append({"spp": k, "render_ms": t_render, "denoise_ms": t_dn, "ms": t_render + t_dn,
+                        "relmse_noisy": e_n, "relmse": e_d, "relmse_debiased": e_d - floor,
+                        "denoise_tflops": flops / (t_dn / 1e3) / 1e12})
+            log(f"denoised {k} spp: noisy {e_n:.3e} -> {e_d:.3e} ({t_render:.1f} + {t_dn:.1f} ms)")
+        res["denoised"] = den
+        res["denoiser_flops_per_frame"] = flops
+        d.close()
+
+    # 5. time to each threshold
+    ttr = []
+    for tau in thresholds:
+        row = {"tau": tau}
+        for key in ("relmse", "relmse_debiased"):
+            hit = next((p for p in plain if p[key] <= tau), None)
+            if hit is not None:
+                pt, how = hit["ms"], "measured"
+            elif key == "relmse_debiased" and c_fit > 0:
+                pt, how = c_fit / tau * ms_per_spp, "extrapolated c/N"
+            else:
+                pt, how = None, "not reached"
+            dh = [p for p in den if p[key] <= tau]
+            dt = min(p["ms"] for p in dh) if dh else None
+            row[key] = {"plain_ms": pt, "plain": how, "denoised_ms": dt,
+                        "speedup": (pt / dt) if (pt and dt) else None}
+        ttr.append(row)
+    res["time_to_relmse"] = ttr
+    return res
+
+
+SMALL = dict(width=480, height=272, ref_spp=1024, plain_max_spp=256, train_views=18, train_iters=300,
+             train_crop=96, train_high_frames=16)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--small", action="store_true", help="a reduced run (480x272, shorter training)")
+    ap.add_argument("--json", default=None)
+    ap.add_argument("--train-iters", type=int, default=None)
+    ap.add_argument("--ref-spp", type=int, default=None)
+    a = ap.parse_args(argv)
+    kw = dict(SMALL) if a.small else {}
+    if a.train_iters:
+        kw["train_iters"] = a.train_iters
+    if a.ref_spp:
+        kw["ref_spp"] = a.ref_spp
+    res = run(**kw)
+    s = json.dumps(res)
+    if a.json:
+        with open(a.json, "w") as f:
+            f.write(s)
+    print(s)
+
+
+if __name__ == "__main__":
+    main()
