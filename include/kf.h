@@ -207,6 +207,19 @@ KF_API int kf_scene_get_instance(kf_scene s, uint32_t index, kf_instance* out); 
 KF_API int kf_instance_release(kf_instance i);
 KF_API int kf_scene_set_clear_color(kf_scene s, const float rgba[4]);      /* setClearColor */
 KF_API int kf_scene_get_clear_color(kf_scene s, float rgba[4]);
+/* Scene::setEnvironmentMap / removeEnvironmentMap (scene.cpp:182-188; uploaded by
+ * uploadEnvironmentMap, scene.cpp:294-310; sampled on every miss by PathTrace.rmiss:14-29
+ * as texture(environmentMap, vec3(-d.y, d.z, -d.x)) instead of the clear colour).
+ * Faces +X, -X, +Y, -Y, +Z, -Z, each size x size texels, rows top to bottom; lookup:
+ * cube-face selection and face coordinates of the Vulkan / GL cube-map rules, bilinear
+ * within the face with clamp-to-edge (no filtering across face seams). */
+KF_API int kf_scene_set_environment_map(kf_scene s, const float* rgba32f, uint32_t size);
+/* The same from RGBA8 texels (srgb != 0: decoded with the sRGB transfer function). */
+KF_API int kf_scene_set_environment_map_rgba8(kf_scene s, const uint8_t* rgba8, uint32_t size, int srgb);
+/* The same from an uncompressed KTX 1.1 cube map file (the format kuafu loads): RGB or
+ * RGBA, 8-bit (UNORM or sRGB), 16-bit float or 32-bit float texels; mip level 0 is used. */
+KF_API int kf_scene_set_environment_map_file(kf_scene s, const char* path);
+KF_API int kf_scene_remove_environment_map(kf_scene s);
 KF_API int kf_scene_mark_geometries_changed(kf_scene s);
 KF_API int kf_scene_mark_instances_changed(kf_scene s);
 
@@ -271,7 +284,9 @@ KF_API int kf_tc_error(uint32_t* out);
  * 32/64/96/128/160 channels) over log radiance, albedo, normal and depth,
  * trained on this renderer's own low-spp / high-spp pairs. ---- */
 typedef struct kf_denoiser_s* kf_denoiser;
-/* A denoiser with He-initialised weights (seeded). Destroy it before its renderer. */
+/* A denoiser with He-initialised weights (seeded), owned by renderer r:
+ * kf_renderer_destroy frees the denoisers still alive, after which their handles are
+ * invalid (kf_denoiser_destroy must not be called on them any more). */
 KF_API int kf_denoiser_create(kf_renderer r, uint32_t seed, kf_denoiser* out);
 KF_API int kf_denoiser_destroy(kf_denoiser d);
 KF_API int kf_denoiser_num_params(kf_denoiser d, uint64_t* out);

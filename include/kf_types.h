@@ -155,6 +155,11 @@ typedef struct kf_flat_scene {
     kf_dir_light_ubo dlight;
     kf_point_lights_ubo plights;
     kf_active_lights_ubo alights;
+    /* environment cube map (NULL = none): faces +X, -X, +Y, -Y, +Z, -Z, each
+     * env_size x env_size linear RGBA32F texels, rows top to bottom */
+    const float* env_rgba32f;
+    uint32_t env_size;
+    uint32_t env_pad;
 } kf_flat_scene;
 
 /* Closest-hit record (what traceRayEXT hands to the hit shaders). */

@@ -406,10 +406,12 @@ class Scene {
             if (g->path == path) return g;
         return nullptr;
     }
-    void setEnvironmentMap(std::string_view) {
-        throw std::runtime_error("cube-map environments are not supported; use setClearColor");
+    // Scene::setEnvironmentMap (scene.cpp:182-186): a KTX 1.1 cube map file
+    void setEnvironmentMap(std::string_view path) {
+        const std::string p(path);
+        detail::check(kf_scene_set_environment_map_file(s_, p.c_str()));
     }
-    void removeEnvironmentMap() {}
+    void removeEnvironmentMap() { detail::check(kf_scene_remove_environment_map(s_)); }
     Camera* createCamera(int w, int h) {
         kf_camera c = nullptr;
         detail::check(kf_scene_create_camera(s_, w, h, &c));

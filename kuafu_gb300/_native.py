@@ -74,7 +74,8 @@ class kf_flat_scene(C.Structure):
                 ("num_instances", C.c_uint32), ("instances", C.POINTER(kf_flat_instance)),
                 ("materials", C.POINTER(kf_material_gpu)), ("num_materials", C.c_uint32),
                 ("num_textures", C.c_uint32), ("textures", C.POINTER(kf_texture_desc)),
-                ("dlight", kf_dir_light_ubo), ("plights", kf_point_lights_ubo), ("alights", kf_active_lights_ubo)]
+                ("dlight", kf_dir_light_ubo), ("plights", kf_point_lights_ubo), ("alights", kf_active_lights_ubo),
+                ("env_rgba32f", c_f32p), ("env_size", C.c_uint32), ("env_pad", C.c_uint32)]
 
 
 class kf_hit(C.Structure):
@@ -187,6 +188,10 @@ PROTOTYPES = {
     "kf_instance_release": (I, [VP]),
     "kf_scene_set_clear_color": (I, [VP, F4]),
     "kf_scene_get_clear_color": (I, [VP, F4]),
+    "kf_scene_set_environment_map": (I, [VP, VP, U32]),
+    "kf_scene_set_environment_map_rgba8": (I, [VP, VP, U32, I]),
+    "kf_scene_set_environment_map_file": (I, [VP, C.c_char_p]),
+    "kf_scene_remove_environment_map": (I, [VP]),
     "kf_scene_mark_geometries_changed": (I, [VP]),
     "kf_scene_mark_instances_changed": (I, [VP]),
     "kf_scene_set_directional_light": (I, [VP, C.POINTER(kf_directional_light)]),

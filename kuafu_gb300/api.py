@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -318,6 +319,25 @@ class Scene:
         N.check(_lib().kf_scene_get_clear_color(self._h, a))
         return tuple(a)
 
+    def setEnvironmentMap(self, faces):
+        """Scene::setEnvironmentMap: a KTX 1.1 cube map path, or a [6, n, n, 4] array
+        (faces +X, -X, +Y, -Y, +Z, -Z; float32 linear or uint8 sRGB)."""
+        if isinstance(faces, (str, bytes, os.PathLike)):
+            N.check(_lib().kf_scene_set_environment_map_file(self._h, os.fsencode(faces)))
+            return
+        a = np.asarray(faces)
+        assert a.ndim == 4 and a.shape[0] == 6 and a.shape[1] == a.shape[2] and a.shape[3] == 4
+        if a.dtype == np.uint8:
+            a = np.ascontiguousarray(a)
+            N.check(_lib().kf_scene_set_environment_map_rgba8(self._h, a.ctypes.data, a.shape[1], 1))
+        else:
+            a = np.ascontiguousarray(a, np.float32)
+            N.check(_lib().kf_scene_set_environment_map(self._h, a.ctypes.data, a.shape[1]))
+        self._env = a
+
+    def removeEnvironmentMap(self):
+        N.check(_lib().kf_scene_remove_environment_map(self._h))
+
     def setDirectionalLight(self, l: DirectionalLight):
         c = N.kf_directional_light(_f3(l.direction), _f3(l.color), float(l.strength), float(l.softness))
         N.check(_lib().kf_scene_set_directional_light(self._h, C.byref(c)))
@@ -380,6 +400,9 @@ class Kuafu:
 
     def close(self):
         if self._h:
+            # the renderer frees the denoisers it still owns: their handles die with it
+            for d in list(getattr(self, "_denoisers", ())):
+                d._h = None
             N.check(_lib().kf_renderer_destroy(self._h))
             self._h = None
 
@@ -497,6 +520,9 @@ class Denoiser:
         N.check(_lib().kf_denoiser_create(renderer._h, int(seed), C.byref(h)))
         self._h = h
         self.renderer = renderer
+        if not hasattr(renderer, "_denoisers"):
+            renderer._denoisers = weakref.WeakSet()
+        renderer._denoisers.add(self)
 
     def close(self):
         if self._h:

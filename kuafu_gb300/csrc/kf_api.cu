@@ -2,6 +2,7 @@
 // host object model. Each function mirrors the kuafu method named in kf.h.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -156,6 +157,10 @@ kf_scene_s::~kf_scene_s() {
 }
 
 kf_renderer_s::~kf_renderer_s() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (kf_denoiser_s* d : denoisers) kf::denoiser_destroy(d);
+    denoisers.clear();
+    denoiser = nullptr;
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
@@ -731,6 +736,145 @@ KF_API int kf_scene_set_clear_color(kf_scene s, const float rgba[4]) {
         frame_reset(s->renderer); // Scene::setClearColor resets frameCount (scene.hpp:101-105)
     });
 }
+namespace {
+void set_env(kf_scene_s* s, std::vector<float>&& texels, uint32_t size) {
+    s->env_texels = std::move(texels);
+    s->env_size = size;
+    ++s->env_version;
+}
+
+float half_to_float(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h >> 15) << 31, exp = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+    uint32_t bits;
+    if (exp == 0) {
+        if (man == 0) {
+            bits = sign;
+        } else { // subnormal: renormalise
+            int e = -1;
+            uint32_t m = man;
+            do {
+                ++e;
+                m <<= 1;
+            } while ((m & 0x400u) == 0);
+            bits = sign | ((uint32_t)(127 - 15 - e) << 23) | ((m & 0x3FFu) << 13);
+        }
+    } else if (exp == 31) {
+        bits = sign | 0x7F800000u | (man << 13);
+    } else {
+        bits = sign | ((exp + 127 - 15) << 23) | (man << 13);
+    }
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+
+// Minimal KTX 1.1 reader (Khronos KTX file format 1.1): uncompressed cube maps, level 0.
+void load_ktx_cube(const char* path, std::vector<float>& out, uint32_t& size) {
+    FILE* f = std::fopen(path, "rb");
+    KF_REQUIRE(f, KF_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    std::vector<uint8_t> b;
+    {
+        uint8_t buf[65536];
+        size_t n;
+        while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) b.insert(b.end(), buf, buf + n);
+        std::fclose(f);
+    }
+    static const uint8_t kId[12] = {0xAB, 'K', 'T', 'X', ' ', '1', '1', 0xBB, '\r', '\n', 0x1A, '\n'};
+    KF_REQUIRE(b.size() >= 64 && std::memcmp(b.data(), kId, 12) == 0, KF_ERR_INVALID_ARGUMENT,
+               std::string("not a KTX 1.1 file: ") + path);
+    uint32_t hv[13];
+    std::memcpy(hv, b.data() + 12, sizeof(hv));
+    const bool swap = hv[0] == 0x01020304u;
+    KF_REQUIRE(swap || hv[0] == 0x04030201u, KF_ERR_INVALID_ARGUMENT, "KTX: bad endianness word");
+    auto rd = [&](uint32_t v) {
+        return swap ? ((v >> 24) | ((v >> 8) & 0xFF00u) | ((v << 8) & 0xFF0000u) | (v << 24)) : v;
+    };
+    const uint32_t gl_type = rd(hv[1]), gl_format = rd(hv[3]), gl_internal = rd(hv[4]);
+    const uint32_t w = rd(hv[6]), h = rd(hv[7]), faces = rd(hv[10]), kv = rd(hv[12]);
+    KF_REQUIRE(faces == 6 && w == h && w > 0, KF_ERR_INVALID_ARGUMENT, "KTX: not a square cube map");
+    const int comps = gl_format == 0x1908u ? 4 : (gl_format == 0x1907u ? 3 : 0); // GL_RGBA, GL_RGB
+    const int tsize = gl_type == 0x1401u ? 1 : (gl_type == 0x140Bu ? 2 : (gl_type == 0x1406u ? 4 : 0));
+    KF_REQUIRE(comps && tsize, KF_ERR_INVALID_ARGUMENT,
+               "KTX: only uncompressed RGB / RGBA with 8-bit, half or float texels are supported");
+    const bool srgb = gl_internal == 0x8C43u || gl_internal == 0x8C41u; // GL_SRGB8_ALPHA8, GL_SRGB8
+    const std::vector<float>& dec = srgb_decode_table();
+    size_t off = 64 + (size_t)kv;
+    KF_REQUIRE(off + 4 <= b.size(), KF_ERR_INVALID_ARGUMENT, "KTX: truncated");
+    uint32_t image_size;
+    std::memcpy(&image_size, b.data() + off, 4);
+    image_size = rd(image_size);
+    off += 4;
+    const size_t row = ((size_t)w * comps * tsize + 3) / 4 * 4; // rows are 4-byte aligned
+    KF_REQUIRE(image_size >= row * h, KF_ERR_INVALID_ARGUMENT, "KTX: face size does not match the header");
+    const size_t face_bytes = ((size_t)image_size + 3) / 4 * 4;
+    KF_REQUIRE(off + 6 * face_bytes <= b.size() + 3, KF_ERR_INVALID_ARGUMENT, "KTX: truncated face data");
+    out.assign((size_t)6 * w * h * 4, 0.0f);
+    for (uint32_t fc = 0; fc < 6; ++fc) {
+        const uint8_t* fb = b.data() + off + fc * face_bytes;
+        for (uint32_t y = 0; y < h; ++y)
+            for (uint32_t x = 0; x < w; ++x) {
+                float* o = out.data() + (((size_t)fc * h + y) * w + x) * 4;
+                o[3] = 1.0f;
+                for (int c = 0; c < comps; ++c) {
+                    const uint8_t* p = fb + y * row + ((size_t)x * comps + c) * tsize;
+                    float v;
+                    if (tsize == 1) {
+                        v = (srgb && c < 3) ? dec[*p] : (float)*p / 255.0f;
+                    } else if (tsize == 2) {
+                        uint16_t hb;
+                        std::memcpy(&hb, p, 2);
+                        if (swap) hb = (uint16_t)((hb >> 8) | (hb << 8));
+                        v = half_to_float(hb);
+                    } else {
+                        uint32_t fb32;
+                        std::memcpy(&fb32, p, 4);
+                        fb32 = rd(fb32);
+                        std::memcpy(&v, &fb32, 4);
+                    }
+                    o[c] = v;
+                }
+            }
+    }
+    size = w;
+}
+} // namespace
+
+KF_API int kf_scene_set_environment_map(kf_scene s, const float* rgba32f, uint32_t size) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(rgba32f && size > 0, "null or empty environment map");
+        REQ(size <= 16384, "environment map faces larger than 16384^2");
+        set_env(s, std::vector<float>(rgba32f, rgba32f + (size_t)6 * size * size * 4), size);
+    });
+}
+KF_API int kf_scene_set_environment_map_rgba8(kf_scene s, const uint8_t* rgba8, uint32_t size, int srgb) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(rgba8 && size > 0, "null or empty environment map");
+        REQ(size <= 16384, "environment map faces larger than 16384^2");
+        const std::vector<float>& dec = srgb_decode_table();
+        std::vector<float> t((size_t)6 * size * size * 4);
+        for (size_t i = 0; i < t.size(); ++i)
+            t[i] = (srgb && (i & 3) != 3) ? dec[rgba8[i]] : (float)rgba8[i] / 255.0f;
+        set_env(s, std::move(t), size);
+    });
+}
+KF_API int kf_scene_set_environment_map_file(kf_scene s, const char* path) {
+    return guarded([&] {
+        check_scene(s);
+        REQ(path, "null path");
+        std::vector<float> t;
+        uint32_t size = 0;
+        load_ktx_cube(path, t, size);
+        set_env(s, std::move(t), size);
+    });
+}
+KF_API int kf_scene_remove_environment_map(kf_scene s) {
+    return guarded([&] {
+        check_scene(s);
+        set_env(s, std::vector<float>(), 0);
+    });
+}
 KF_API int kf_scene_get_clear_color(kf_scene s, float rgba[4]) {
     return guarded([&] {
         check_scene(s);
@@ -912,6 +1056,8 @@ KF_API int kf_scene_export(kf_scene s, kf_flat_scene* out) {
         out->textures = s->x_texs.data();
         out->num_textures = (uint32_t)s->x_texs.size();
         scene_light_ubos(s, &out->dlight, &out->plights, &out->alights);
+        out->env_rgba32f = s->env_size ? s->env_texels.data() : nullptr;
+        out->env_size = s->env_size;
     });
 }
 
@@ -1075,13 +1221,18 @@ KF_API int kf_denoiser_create(kf_renderer r, uint32_t seed, kf_denoiser* out) {
         REQ(r && out, "null argument");
         require_device(r);
         KF_CUDA_CHECK(cudaSetDevice(r->device));
-        *out = denoiser_create(r, seed);
+        kf_denoiser_s* d = denoiser_create(r, seed);
+        r->denoisers.push_back(d);
+        *out = d;
     });
 }
 KF_API int kf_denoiser_destroy(kf_denoiser d) {
     return guarded([&] {
         if (!d) return;
         kf_renderer_s* r = denoiser_renderer(d);
+        auto it = std::find(r->denoisers.begin(), r->denoisers.end(), d);
+        REQ(it != r->denoisers.end(), "unknown denoiser");
+        r->denoisers.erase(it);
         if (r->denoiser == d) r->denoiser = nullptr;
         cudaStreamSynchronize(r->stream);
         denoiser_destroy(d);

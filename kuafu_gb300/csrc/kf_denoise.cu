@@ -28,80 +28,137 @@ namespace {
 using bf16 = __nv_bfloat16;
 
 // ---------------------------------------------------------------------------
-// Elementwise kernels (memory-bound, NHWC with channel stride / offset).
+// Elementwise kernels (HBM-bound, NHWC with channel stride / offset). Channel counts,
+// strides and offsets of pooled / upsampled tensors are multiples of 8, so each thread
+// moves 8 channels (16 bytes) per access.
 // ---------------------------------------------------------------------------
+struct F8 {
+    float v[8];
+};
+__device__ __forceinline__ F8 ld8(const bf16* p) {
+    const uint4 q = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+    F8 f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 t = __bfloat1622float2(h[k]);
+        f.v[2 * k] = t.x;
+        f.v[2 * k + 1] = t.y;
+    }
+    return f;
+}
+__device__ __forceinline__ void st8(bf16* p, const F8& f) {
+    uint4 q;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&q);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(f.v[2 * k], f.v[2 * k + 1]);
+    *reinterpret_cast<uint4*>(p) = q;
+}
+
+// y (dense, H/2 x W/2) = 2x2 average of x[slice] (H x W)
 __global__ void k_pool_fwd(const bf16* __restrict__ x, int xs, int xo, int C, int N, int H, int W, bf16* y) {
-    const int Ho = H / 2, Wo = W / 2;
-    const size_t total = (size_t)N * Ho * Wo * C;
+    const int Ho = H / 2, Wo = W / 2, G = C / 8;
+    const size_t total = (size_t)N * Ho * Wo * G;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t r = i / C;
-        const int xw = (int)(r % Wo);
-        r /= Wo;
-        const int yh = (int)(r % Ho);
-        const int n = (int)(r / Ho);
-        float s = 0.0f;
-        for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx)
-                s += __bfloat162float(x[(((size_t)n * H + 2 * yh + dy) * W + 2 * xw + dx) * xs + xo + c]);
-        y[i] = __float2bfloat16_rn(0.25f * s);
+        const int g = (int)(i % G);
+        const size_t pix = i / G; // (n, yh, xw) of the output
+        const int xw = (int)(pix % Wo);
+        const size_t ny = pix / Wo; // n * Ho + yh
+        const size_t row0 = (2 * ny) * W + 2 * xw; // n * H + 2 yh == 2 * (n * Ho + yh)
+        F8 a = ld8(x + row0 * xs + xo + 8 * g), b = ld8(x + (row0 + 1) * xs + xo + 8 * g);
+        const F8 c = ld8(x + (row0 + W) * xs + xo + 8 * g), d = ld8(x + (row0 + W + 1) * xs + xo + 8 * g);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a.v[k] = 0.25f * (((a.v[k] + b.v[k]) + c.v[k]) + d.v[k]);
+        st8(y + pix * C + 8 * g, a);
     }
 }
 
 // gx (dense, H x W) = broadcast(gy / 4) + gskip[slice] (optional)
 __global__ void k_pool_bwd_add(const bf16* __restrict__ gy, const bf16* __restrict__ gskip, int ss, int so, int C,
                                int N, int H, int W, bf16* gx) {
-    const size_t total = (size_t)N * H * W * C;
+    const int G = C / 8;
+    const size_t total = (size_t)N * H * W * G;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t r = i / C;
-        const int xw = (int)(r % W);
-        r /= W;
-        const int yh = (int)(r % H);
-        const int n = (int)(r / H);
-        float v = 0.25f * __bfloat162float(gy[(((size_t)n * (H / 2) + yh / 2) * (W / 2) + xw / 2) * C + c]);
-        if (gskip) v += __bfloat162float(gskip[(((size_t)n * H + yh) * W + xw) * ss + so + c]);
-        gx[i] = __float2bfloat16_rn(v);
+        const int g = (int)(i % G);
+        const size_t pix = i / G;
+        const int xw = (int)(pix % W);
+        const size_t ny = pix / W; // n * H + y
+        const size_t low = (ny / 2) * (W / 2) + xw / 2;
+        F8 v = ld8(gy + low * C + 8 * g);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v.v[k] *= 0.25f;
+        if (gskip) {
+            const F8 sk = ld8(gskip + pix * ss + so + 8 * g);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v.v[k] += sk.v[k];
+        }
+        st8(gx + pix * C + 8 * g, v);
     }
 }
 
 // nearest 2x upsampling of x (dense, H/2 x W/2) into y[slice] (H x W)
 __global__ void k_up_fwd(const bf16* __restrict__ x, int C, int N, int H, int W, bf16* y, int ys, int yo) {
-    const size_t total = (size_t)N * H * W * C;
+    const int Ho = H / 2, Wo = W / 2, G = C / 8;
+    const size_t total = (size_t)N * Ho * Wo * G;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t r = i / C;
-        const int xw = (int)(r % W);
-        r /= W;
-        const int yh = (int)(r % H);
-        const int n = (int)(r / H);
-        y[(((size_t)n * H + yh) * W + xw) * ys + yo + c] =
-            x[(((size_t)n * (H / 2) + yh / 2) * (W / 2) + xw / 2) * C + c];
+        const int g = (int)(i % G);
+        const size_t pix = i / G;
+        const int xw = (int)(pix % Wo);
+        const size_t ny = pix / Wo;
+        const uint4 q = *reinterpret_cast<const uint4*>(x + pix * C + 8 * g);
+        const size_t row0 = (2 * ny) * W + 2 * xw;
+        *reinterpret_cast<uint4*>(y + row0 * ys + yo + 8 * g) = q;
+        *reinterpret_cast<uint4*>(y + (row0 + 1) * ys + yo + 8 * g) = q;
+        *reinterpret_cast<uint4*>(y + (row0 + W) * ys + yo + 8 * g) = q;
+        *reinterpret_cast<uint4*>(y + (row0 + W + 1) * ys + yo + 8 * g) = q;
     }
 }
 
 // gx (dense, H/2 x W/2) = sum of the 2x2 block of gy[slice] (H x W)
 __global__ void k_up_bwd(const bf16* __restrict__ gy, int gs, int go, int C, int N, int H, int W, bf16* gx) {
-    const int Ho = H / 2, Wo = W / 2;
-    const size_t total = (size_t)N * Ho * Wo * C;
+    const int Ho = H / 2, Wo = W / 2, G = C / 8;
+    const size_t total = (size_t)N * Ho * Wo * G;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        size_t r = i / C;
-        const int xw = (int)(r % Wo);
-        r /= Wo;
-        const int yh = (int)(r % Ho);
-        const int n = (int)(r / Ho);
-        float s = 0.0f;
-        for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx)
-                s += __bfloat162float(gy[(((size_t)n * H + 2 * yh + dy) * W + 2 * xw + dx) * gs + go + c]);
-        gx[i] = __float2bfloat16_rn(s);
+        const int g = (int)(i % G);
+        const size_t pix = i / G;
+        const int xw = (int)(pix % Wo);
+        const size_t ny = pix / Wo;
+        const size_t row0 = (2 * ny) * W + 2 * xw;
+        F8 a = ld8(gy + row0 * gs + go + 8 * g), b = ld8(gy + (row0 + 1) * gs + go + 8 * g);
+        const F8 c = ld8(gy + (row0 + W) * gs + go + 8 * g), d = ld8(gy + (row0 + W + 1) * gs + go + 8 * g);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a.v[k] = ((a.v[k] + b.v[k]) + c.v[k]) + d.v[k];
+        st8(gx + pix * C + 8 * g, a);
     }
 }
 
 // dz[p][c] = (c < C) ? gy[p][c] * (relu ? y[p][c] > 0 : 1) : 0   for c < Ck (dense, Ck channels)
 __global__ void k_relu_mask(const bf16* __restrict__ gy, int gs, int go, const bf16* __restrict__ y, int ys, int yo,
                             int C, int Ck, size_t P, int relu, bf16* dz) {
+    const bool vec = (C % 8) == 0 && (gs % 8) == 0 && (go % 8) == 0 && (!relu || ((ys % 8) == 0 && (yo % 8) == 0));
+    if (vec) {
+        const int G = Ck / 8, Gc = C / 8;
+        const size_t total = P * G;
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+            const int g = (int)(i % G);
+            const size_t p = i / G;
+            F8 v;
+            if (g < Gc) {
+                v = ld8(gy + p * gs + go + 8 * g);
+                if (relu) {
+                    const F8 m = ld8(y + p * ys + yo + 8 * g);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (!(m.v[k] > 0.0f)) v.v[k] = 0.0f;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v.v[k] = 0.0f;
+            }
+            st8(dz + p * Ck + 8 * g, v);
+        }
+        return;
+    }
     const size_t total = P * Ck;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int c = (int)(i % Ck);
@@ -225,7 +282,13 @@ __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __
             f[10] = spp_feature;
         }
         bf16* o = out + i * 32;
-        for (int c = 0; c < 32; ++c) o[c] = __float2bfloat16_rn(f[c]);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            F8 q;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) q.v[k] = f[8 * g + k];
+            st8(o + 8 * g, q);
+        }
         if (base) base[i] = make_float4(f[0], f[1], f[2], 0.0f);
     }
 }
@@ -551,11 +614,11 @@ TRef T(Acts& a, int k) { return TRef{a.at(k), kT[k].c, 0, kT[k].c}; }
 TRef S(Acts& a, int k, int off, int cnt) { return TRef{a.at(k), kT[k].c, off, cnt}; }
 
 void pool_fwd(Ctx& c, TRef x, int level, TRef y) {
-    const size_t n = c.P(level + 1) * x.c;
+    const size_t n = c.P(level + 1) * x.c / 8;
     k_pool_fwd<<<grid_for(n), 256, 0, c.st>>>(x.p, x.cs, x.co, x.c, c.n, c.H(level), c.W(level), y.p);
 }
 void up_fwd(Ctx& c, TRef x, int level_hi, TRef y) {
-    const size_t n = c.P(level_hi) * x.c;
+    const size_t n = c.P(level_hi + 1) * x.c / 8;
     k_up_fwd<<<grid_for(n), 256, 0, c.st>>>(x.p, x.c, c.n, c.H(level_hi), c.W(level_hi), y.p, y.cs, y.co);
 }
 
@@ -599,12 +662,12 @@ void forward(Ctx& c, const float4* base) {
 }
 
 void pool_bwd_add(Ctx& c, TRef gy_low, TRef gskip, int level_hi, TRef gx) {
-    const size_t n = c.P(level_hi) * gx.c;
+    const size_t n = c.P(level_hi) * gx.c / 8;
     k_pool_bwd_add<<<grid_for(n), 256, 0, c.st>>>(gy_low.p, gskip.p, gskip.cs, gskip.co, gx.c, c.n, c.H(level_hi),
                                                    c.W(level_hi), gx.p);
 }
 void up_bwd(Ctx& c, TRef gy_slice, int level_hi, TRef gx_low) {
-    const size_t n = c.P(level_hi + 1) * gx_low.c;
+    const size_t n = c.P(level_hi + 1) * gx_low.c / 8;
     k_up_bwd<<<grid_for(n), 256, 0, c.st>>>(gy_slice.p, gy_slice.cs, gy_slice.co, gx_low.c, c.n, c.H(level_hi),
                                              c.W(level_hi), gx_low.p);
 }

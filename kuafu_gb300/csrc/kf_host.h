@@ -79,6 +79,8 @@ struct SceneGpu {
     kf::DeviceBuffer<uint4> tex_info;
     kf::DeviceBuffer<uchar4> texels;
     kf::DeviceBuffer<float> srgb_decode;
+    kf::DeviceBuffer<float4> env;
+    uint64_t built_env_version = 0;
     std::vector<uint32_t> blas_root;                 // per geometry
     std::vector<std::array<float, 6>> blas_box;      // per geometry object-space box
     std::vector<uint32_t> tri_offset, vert_offset;   // per geometry
@@ -96,6 +98,10 @@ struct kf_scene_s {
     std::vector<kf_geometry_s*> geometries;
     std::vector<kf_instance_s*> instances;
     float clear_color[4] = {0, 0, 0, 1};
+    // environment cube map: 6 faces of env_size^2 linear RGBA texels (empty = none)
+    std::vector<float> env_texels;
+    uint32_t env_size = 0;
+    uint64_t env_version = 0;
     bool has_dir_light = false;
     kf_directional_light dir_light{};
     std::vector<kf_light_s*> point_lights;
@@ -149,8 +155,10 @@ struct kf_renderer_s {
     std::string graph_key;
     // events for profiling
     cudaEvent_t ev[8] = {};
-    // learned denoiser used by run() when cfg.use_denoiser is set (not owned)
+    // learned denoiser used by run() when cfg.use_denoiser is set
     kf_denoiser_s* denoiser = nullptr;
+    // every denoiser created on this renderer (owned: freed by the renderer's destructor)
+    std::vector<kf_denoiser_s*> denoisers;
     ~kf_renderer_s();
 };
 

@@ -310,7 +310,7 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
     f.pc.frame_count = r->frame_count;
     f.pc.spp = spp;
     f.pc.max_path_depth = r->cfg.path_depth;
-    f.pc.use_env_map = 0;
+    f.pc.use_env_map = s->env_size ? 1u : 0u;
     f.pc.russian_roulette = r->cfg.russian_roulette;
     f.pc.rr_min_bounces = r->cfg.rr_min_bounces;
     f.pc.nee = r->cfg.nee;

@@ -284,6 +284,16 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         G.built_texture_version = g_texture_version;
         ++G.generation;
     }
+    if (G.built_env_version != s->env_version) {
+        // uploadEnvironmentMap (scene.cpp:294-310)
+        if (s->env_size) {
+            G.env.upload(reinterpret_cast<const float4*>(s->env_texels.data()), s->env_texels.size() / 4, st);
+        } else {
+            G.env.release();
+        }
+        G.built_env_version = s->env_version;
+        ++G.generation;
+    }
     if (rebuilt_geom || G.built_inst_stamp != s->inst_stamp) {
         built_any = true;
         const size_t ni = s->instances.size();
@@ -388,6 +398,8 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
     v.tex_info = G.tex_info.ptr;
     v.texels = G.texels.ptr;
     v.srgb_decode = G.srgb_decode.ptr;
+    v.env = s->env_size ? G.env.ptr : nullptr;
+    v.env_size = s->env_size;
     v.num_instances = (uint32_t)s->instances.size();
     v.has_tlas = G.tlas_node_count > 0 ? 1u : 0u;
     v.num_textures = (uint32_t)g_textures.size();

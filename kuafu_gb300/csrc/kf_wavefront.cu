@@ -422,6 +422,46 @@ __device__ __forceinline__ v3 uniformSphereSampling(Stream& st, const PathKey& p
     return p;
 }
 
+// Environment lookup of PathTrace.rmiss:14-29: texture(environmentMap, vec3(-d.y, d.z, -d.x)).
+// Face selection by the major axis and face coordinates (sc, tc) of the Vulkan / GL cube
+// rules; bilinear within the face, clamp to edge.
+__device__ v3 env_lookup(const SceneDev& s, v3 d) {
+    const float rx = -d.y, ry = d.z, rz = -d.x;
+    const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
+    uint32_t face;
+    float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        ma = ax;
+        face = rx >= 0.0f ? 0u : 1u;
+        sc = rx >= 0.0f ? -rz : rz;
+        tc = -ry;
+    } else if (ay >= az) {
+        ma = ay;
+        face = ry >= 0.0f ? 2u : 3u;
+        sc = rx;
+        tc = ry >= 0.0f ? rz : -rz;
+    } else {
+        ma = az;
+        face = rz >= 0.0f ? 4u : 5u;
+        sc = rz >= 0.0f ? rx : -rx;
+        tc = -ry;
+    }
+    const uint32_t n = s.env_size;
+    const float fs = 0.5f * (sc / ma + 1.0f), ft = 0.5f * (tc / ma + 1.0f);
+    const float x = fs * (float)n - 0.5f, y = ft * (float)n - 0.5f;
+    const float fx0 = floorf(x), fy0 = floorf(y);
+    const float wx = x - fx0, wy = y - fy0;
+    const int ix = (int)fx0, iy = (int)fy0, hi = (int)n - 1;
+    const uint32_t x0 = (uint32_t)min(max(ix, 0), hi), x1 = (uint32_t)min(max(ix + 1, 0), hi);
+    const uint32_t y0 = (uint32_t)min(max(iy, 0), hi), y1 = (uint32_t)min(max(iy + 1, 0), hi);
+    const float4* fp = s.env + (size_t)face * n * n;
+    const float4 t00 = __ldg(fp + (size_t)y0 * n + x0), t10 = __ldg(fp + (size_t)y0 * n + x1);
+    const float4 t01 = __ldg(fp + (size_t)y1 * n + x0), t11 = __ldg(fp + (size_t)y1 * n + x1);
+    const v3 top = mk(t00.x, t00.y, t00.z) * (1.0f - wx) + mk(t10.x, t10.y, t10.z) * wx;
+    const v3 bot = mk(t01.x, t01.y, t01.z) * (1.0f - wx) + mk(t11.x, t11.y, t11.z) * wx;
+    return top * (1.0f - wy) + bot * wy;
+}
+
 // Texture lookup: bilinear, repeat, optional sRGB decode (vkCore.hpp:585,619-637).
 __device__ v3 texture_rgb(const SceneDev& s, int id, float u, float v) {
     if (id < 0 || (uint32_t)id >= s.num_textures) return splat(1.0f);
@@ -634,8 +674,9 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
             v3 color = mk(col4.x, col4.y, col4.z);
             const v3 rayD = mk(qd.x, qd.y, qd.z);
             if (inst == kMiss) {
-                // PathTrace.rmiss:12-31 (clear colour; environment cube maps are not provided)
-                const v3 emission = ld3(f.pc.clear_color) * f.pc.clear_color[3];
+                // PathTrace.rmiss:12-31: environment map, else clear colour
+                const v3 emission = (f.pc.use_env_map && s.env) ? env_lookup(s, rayD)
+                                                                 : ld3(f.pc.clear_color) * f.pc.clear_color[3];
                 color = color + emission * wold;
                 w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
             } else {

@@ -29,6 +29,8 @@ struct SceneDev {
     const uint4* tex_info;           // per texture {texel offset, width, height, srgb}
     const uchar4* texels;
     const float* srgb_decode;        // 256 entries
+    const float4* env;               // environment cube map: 6 faces of env_size^2 texels (null = none)
+    uint32_t env_size;
     uint32_t num_instances;
     uint32_t has_tlas;
     uint32_t num_textures;

@@ -106,8 +106,8 @@ def _accumulate(r, cfg, cam, seed, spp_total, frame_spp):
 
 
 def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp=8, plain_max_spp=1024,
-        train_views=64, train_size=256, train_high_spp=64, train_high_frames=64, train_iters=3000,
-        train_batch=8, train_crop=128, lr=1e-3, denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256),
+        train_views=66, train_size=256, train_high_spp=64, train_high_frames=64, train_iters=4000,
+        train_batch=8, train_crop=128, lr=1e-3, denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024),
         thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3), depth=5, log=print) -> dict:
     cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
     res = {"scene": "cornell", "width": width, "height": height, "depth": depth, "eps": EPS}

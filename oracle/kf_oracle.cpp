@@ -576,6 +576,47 @@ template <class R> V3<R> texture_rgb(const kf_flat_scene& s, int id, R u, R v) {
     return V3<R>((R)out[0], (R)out[1], (R)out[2]);
 }
 
+// PathTrace.rmiss:14-29: texture(environmentMap, vec3(-d.y, d.z, -d.x)) of a cube map.
+// Face by the major axis, face coordinates (sc, tc) of the Vulkan / GL cube-map rules
+// (Vulkan spec "Cube Map Face Selection"), bilinear within the face, clamp to edge.
+// Evaluated in float whatever the oracle precision (a texture unit filters in float).
+static void env_lookup(const kf_flat_scene& s, const float d[3], float out[3]) {
+    const float rx = -d[1], ry = d[2], rz = -d[0];
+    const float ax = std::fabs(rx), ay = std::fabs(ry), az = std::fabs(rz);
+    uint32_t face;
+    float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        ma = ax;
+        face = rx >= 0.0f ? 0u : 1u;
+        sc = rx >= 0.0f ? -rz : rz;
+        tc = -ry;
+    } else if (ay >= az) {
+        ma = ay;
+        face = ry >= 0.0f ? 2u : 3u;
+        sc = rx;
+        tc = ry >= 0.0f ? rz : -rz;
+    } else {
+        ma = az;
+        face = rz >= 0.0f ? 4u : 5u;
+        sc = rz >= 0.0f ? rx : -rx;
+        tc = -ry;
+    }
+    const uint32_t n = s.env_size;
+    const float fs = 0.5f * (sc / ma + 1.0f), ft = 0.5f * (tc / ma + 1.0f);
+    const float x = fs * (float)n - 0.5f, y = ft * (float)n - 0.5f;
+    const float fx0 = std::floor(x), fy0 = std::floor(y);
+    const float wx = x - fx0, wy = y - fy0;
+    const int ix = (int)fx0, iy = (int)fy0, hi = (int)n - 1;
+    auto cl = [hi](int i) { return (size_t)std::min(std::max(i, 0), hi); };
+    const size_t x0 = cl(ix), x1 = cl(ix + 1), y0 = cl(iy), y1 = cl(iy + 1);
+    const float* fp = s.env_rgba32f + (size_t)face * n * n * 4;
+    for (int c = 0; c < 3; ++c) {
+        const float top = fp[(y0 * n + x0) * 4 + c] * (1.0f - wx) + fp[(y0 * n + x1) * 4 + c] * wx;
+        const float bot = fp[(y1 * n + x0) * 4 + c] * (1.0f - wx) + fp[(y1 * n + x1) * 4 + c] * wx;
+        out[c] = top * (1.0f - wy) + bot * wy;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Shader library (base/Random.glsl, base/Sampling.glsl).
 // ---------------------------------------------------------------------------
@@ -1022,9 +1063,15 @@ void render_pixel(Ctx& cx, const kf_oracle_view& view, uint32_t px, uint32_t py,
                 cx.rays_extension++;
             }
             if (!hit) {
-                // PathTrace.rmiss:12-31 (environment map path not supported: clear colour)
-                ray.emission = V3<R>((R)pc.clear_color[0], (R)pc.clear_color[1], (R)pc.clear_color[2]) *
-                               (R)pc.clear_color[3];
+                // PathTrace.rmiss:12-31: environment map, else clear colour
+                if (pc.use_env_map && cx.s->env_rgba32f && cx.s->env_size) {
+                    float e[3];
+                    env_lookup(*cx.s, dg, e);
+                    ray.emission = V3<R>((R)e[0], (R)e[1], (R)e[2]);
+                } else {
+                    ray.emission = V3<R>((R)pc.clear_color[0], (R)pc.clear_color[1], (R)pc.clear_color[2]) *
+                                   (R)pc.clear_color[3];
+                }
                 ray.depth = pc.max_path_depth + 1;
             } else {
                 closestHit<R>(cx, rng, ray, h, og, dg);

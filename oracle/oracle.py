@@ -81,13 +81,14 @@ def load():
     return _lib
 
 
-def push_constants(spp, depth, clear=(0, 0, 0, 1), rr=False, rr_min=4, frame_count=0) -> N.kf_push_constants:
+def push_constants(spp, depth, clear=(0, 0, 0, 1), rr=False, rr_min=4, frame_count=0,
+                   env=False) -> N.kf_push_constants:
     pc = N.kf_push_constants()
     pc.clear_color[:] = [float(x) for x in clear]
     pc.frame_count = frame_count
     pc.spp = spp
     pc.max_path_depth = depth
-    pc.use_env_map = 0
+    pc.use_env_map = int(bool(env))
     pc.russian_roulette = int(rr)
     pc.rr_min_bounces = rr_min
     pc.nee = 1

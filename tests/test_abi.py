@@ -55,6 +55,19 @@ def test_host_only_renderer_refuses_to_render():
     assert e.value.code == 7  # KF_ERR_NO_DEVICE: no CPU fallback
 
 
+def test_host_only_renderer_has_no_denoiser_and_no_tensor_kernels():
+    r = host_renderer()
+    with pytest.raises(N.KfError) as e:
+        api.Denoiser(r)
+    assert e.value.code == 7
+    # use_denoiser without an attached denoiser is a state error before anything renders
+    r.config.setUseDenoiser(True)
+    r.applyConfig()
+    with pytest.raises(N.KfError):
+        r.run()
+    r.close()
+
+
 def test_config_defaults_are_kuafus():
     c = api.Config()._c
     assert (c.spp, c.path_depth, c.max_path_depth, c.russian_roulette, c.rr_min_bounces) == (32, 8, 12, 1, 4)

@@ -21,14 +21,15 @@ def _camera_index(scene_cams_before):
     return scene_cams_before
 
 
-def _render_pair(r, cam, spp, depth, rr=False, rr_min=4, clear=(0, 0, 0, 1), cam_index=1, use_bvh=False, frame=0):
+def _render_pair(r, cam, spp, depth, rr=False, rr_min=4, clear=(0, 0, 0, 1), cam_index=1, use_bvh=False, frame=0,
+                 env=False):
     r.run()
     paths = r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp)
     hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)
     rgba = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
     w, h = cam._size()
     flat = r.getScene().export()
-    pc = O.push_constants(spp, depth, clear=clear, rr=rr, rr_min=rr_min)
+    pc = O.push_constants(spp, depth, clear=clear, rr=rr, rr_min=rr_min, env=env)
     ref = O.render(flat, cam.ubo(), w, h, pc, seed=r.config._c.seed, frame=frame, camera_index=cam_index,
                    use_bvh=use_bvh)
     return paths, hits, rgba, ref
@@ -125,6 +126,72 @@ def test_icospheres_with_lights_bvh_parity(traversal):
         st = r.stats()
         assert st.rays_shadow > 0 and st.rays_extension > 0
         assert st.rays_primary == 96 * 64 * spp
+
+
+def _smooth_env(n, seed):
+    """Six n x n faces of smooth positive radiance (float32 RGBA)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:n, 0:n] / max(n - 1, 1)
+    faces = np.ones((6, n, n, 4), np.float32)
+    for f in range(6):
+        for c in range(3):
+            a, b, ph = rng.uniform(0.5, 3.0, 3)
+            faces[f, :, :, c] = 0.3 + 0.25 * np.sin(a * x * 6.28 + ph) * np.cos(b * y * 6.28) + 0.1 * f
+    return faces
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_environment_map_parity(traversal):
+    """PathTrace.rmiss with useEnvironmentMap: misses return the cube-map lookup of (-d.y, d.z, -d.x)."""
+    spp, depth = 2, 4
+    cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
+    cfg.setDebugOutputs(True)
+    cfg.setTraversal(traversal)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.icospheres(r, 96, 64, count=24, level=2)
+        r.getScene().setEnvironmentMap(_smooth_env(16, 3))
+        paths, hits, rgba, ref = _render_pair(r, cam, spp, depth, clear=(0.1, 0.1, 0.1, 1.0), use_bvh=True,
+                                              env=True)
+        assert np.array_equal(hits["instance"], ref["hits"]["instance"])
+        _check_paths(paths, ref["paths"])
+        miss = hits["instance"] == 0xFFFFFFFF
+        assert miss.mean() > 0.5
+        # escaped camera rays see the map, not the clear colour
+        assert not np.allclose(paths[..., :3][miss], 0.1)
+
+
+def test_textured_materials_and_projector_parity():
+    """Diffuse / roughness textures (rchit:338-360) and a textured active light, i.e. a
+    projector (rchit:262-316, texture(tex, uv) of proj * view * worldPos), against the oracle."""
+    spp, depth = 4, 3
+    cfg = scenes.cornell_config(spp=spp, depth=depth, debug=True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, 64, 48)
+        s = r.getScene()
+        rng = np.random.default_rng(5)
+        checker = np.zeros((16, 16, 4), np.uint8)
+        checker[..., 3] = 255
+        checker[::2, ::2, :3] = 220
+        checker[1::2, 1::2, :3] = 220
+        checker[..., 0] |= rng.integers(0, 30, (16, 16), dtype=np.uint8)
+        tex = api.createTexture(checker, srgb=True)
+        rough = api.createTexture(rng.integers(0, 255, (8, 8, 4), dtype=np.uint8), srgb=False)
+        mat = api.NiceMaterial(diffuseColor=(0.8, 0.8, 0.8), roughness=0.5, diffuseTex=tex, roughnessTex=rough)
+        panel = api.createYZPlane(True, mat)
+        s.submitGeometry(panel)
+        s.submitGeometryInstance(api.instance(panel, scenes.translate(0.95, 0, 0) @ scenes.rot_axis("z", 180) @
+                                              scenes.scale(1, 0.8, 0.8)))
+        # a dot-pattern projector (5 % density, seeded) aimed at the back wall
+        dots = np.zeros((64, 64, 4), np.uint8)
+        dots[..., 3] = 255
+        dots[..., :3][rng.random((64, 64)) < 0.05] = 255
+        pat = api.createTexture(dots, srgb=False)
+        view = scenes.look_at_view((-0.5, 0.0, 0.2), (1.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+        s.addActiveLight(api.ActiveLight(viewMat=view, fov=np.radians(50), strength=5, softness=0,
+                                         texID=pat))
+        paths, hits, rgba, ref = _render_pair(r, cam, spp, depth)
+        assert np.array_equal(hits["instance"], ref["hits"]["instance"])
+        _check_paths(paths, ref["paths"])
 
 
 def test_traversal_counters():
