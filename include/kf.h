@@ -257,7 +257,15 @@ KF_API int kf_camera_reset_view(kf_camera c);                              /* re
 KF_API int kf_camera_get_size(kf_camera c, int* width, int* height);
 KF_API int kf_camera_get_ubo(kf_camera c, kf_camera_ubo* out);             /* uploadCameraBuffer, scene.cpp:236-250 */
 
-/* ---- batched offscreen rendering: many cameras / scenes in one launch sequence ---- */
+/* ---- batched offscreen rendering: many cameras / scenes in one wavefront ----
+ * kuafu renders one camera of the current scene per run(); SAPIEN renders many views
+ * by calling it in turn. Here the views of any scenes of this renderer are traced
+ * together: their paths form one path space, each bounce is one launch of each kernel
+ * over all views, and the whole sequence is captured in one CUDA graph (replayed while
+ * the batch's layout is unchanged). Each view is an independent single frame
+ * (frameCount -1, no blending), written to its camera's targets exactly as
+ * kf_renderer_run would write it for the same frame word; all views of a batch share
+ * one frame word. spp 0 = the config's spp. A camera may appear once per batch. */
 typedef struct kf_batch_item {
     kf_scene scene;
     kf_camera camera;

@@ -345,16 +345,19 @@ KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint
         REQ(r && (items || count == 0), "null argument");
         require_device(r);
         KF_CUDA_CHECK(cudaSetDevice(r->device));
+        std::vector<kf_batch_item> v(items, items + count);
         for (uint32_t i = 0; i < count; ++i) {
-            kf_scene_s* s = check_scene(items[i].scene);
-            kf_camera_s* c = check_camera(items[i].camera);
+            kf_scene_s* s = check_scene(v[i].scene);
+            kf_camera_s* c = check_camera(v[i].camera);
             REQ(c->scene == s, "batch camera does not belong to its scene");
+            REQ(std::find_if(r->scenes.begin(), r->scenes.end(), [&](auto& p) { return p.get() == s; }) !=
+                    r->scenes.end(),
+                "batch scene does not belong to this renderer");
+            for (uint32_t j = 0; j < i; ++j) REQ(v[j].camera != c, "a camera appears twice in one batch");
             camera_update_view(c);
-            const int32_t saved = r->frame_count;
-            r->frame_count = -1; // batched views are independent single frames
-            render_frame(r, s, c, items[i].spp ? items[i].spp : r->cfg.spp);
-            r->frame_count = saved;
+            if (!v[i].spp) v[i].spp = r->cfg.spp;
         }
+        if (count) render_batch(r, v.data(), count);
     });
 }
 
@@ -402,13 +405,13 @@ KF_API int kf_renderer_download_aov(kf_renderer r, kf_camera cam, int kind, void
             case KF_AOV_DEPTH_F32: src = c->depth.ptr; need = npix * 4; break;
             case KF_AOV_SUM_F64: src = c->sum64.ptr; need = npix * 32; break;
             case KF_AOV_PATH_RADIANCE:
-                src = r->wave.radiance.ptr;
-                need = (size_t)r->stats.last_spp * npix * 16;
+                src = r->wave.radiance.ptr + c->last_path_start;
+                need = (size_t)c->last_spp * npix * 16;
                 break;
             case KF_AOV_PRIMARY_HITS:
                 KF_REQUIRE(r->cfg.debug_outputs, KF_ERR_STATE, "primary hits need debug_outputs = 1");
-                src = r->wave.primary.ptr;
-                need = (size_t)r->stats.last_spp * npix * sizeof(kf_hit);
+                src = r->wave.primary.ptr + c->last_path_start;
+                need = (size_t)c->last_spp * npix * sizeof(kf_hit);
                 break;
             case KF_AOV_DENOISED_F32:
                 KF_REQUIRE(c->denoised.count == npix, KF_ERR_STATE, "no denoised frame for this camera");

@@ -61,6 +61,9 @@ struct kf_camera_s {
     kf::DeviceBuffer<uchar4> bgra;
     bool has_frame = false;
     int target_w = 0, target_h = 0;
+    // where this camera's paths of its last frame sit in the renderer's per-path buffers
+    uint64_t last_path_start = 0;
+    uint32_t last_spp = 0;
 };
 
 // Device copy of a scene, rebuilt when its geometry / instances change.
@@ -119,6 +122,29 @@ struct kf_scene_s {
     ~kf_scene_s();
 };
 
+// A batched launch: the scenes of the batch concatenated into one set of geometry / BVH
+// pools (indices rebased), so that one wavefront serves every view; each view keeps its
+// own TLAS root, lights, environment and render targets in its ItemDev.
+struct BatchState {
+    std::vector<kf_scene_s*> scenes;   // distinct scenes, in order of first use
+    std::vector<uint64_t> generations; // their SceneGpu generations when the pools were built
+    kf::DeviceBuffer<float4> verts;
+    kf::DeviceBuffer<uint32_t> indices, matidx, tlas_inst;
+    kf::DeviceBuffer<uint4> geom;
+    kf::DeviceBuffer<kf::InstanceRec> inst;
+    kf::DeviceBuffer<kf::Node4> blas_nodes, tlas_nodes;
+    kf::DeviceBuffer<kf::Tri> tris;
+    std::vector<uint32_t> roots;       // per scene: TLAS root in tlas_nodes (kNoRoot: empty)
+    kf::SceneDev view{};
+    uint64_t generation = 0;           // bumped whenever a pool may have moved
+    kf::DeviceBuffer<kf::ItemDev> items;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::string graph_key;
+    ~BatchState() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    }
+};
+
 // Wavefront buffers sized for one chunk of paths.
 struct WaveBuffers {
     kf::DeviceBuffer<float4> q_o0, q_o1, q_d0, q_d1, hit, weight, nee_w, contrib, sq_o, sq_d;
@@ -128,6 +154,7 @@ struct WaveBuffers {
     kf::DeviceBuffer<float4> radiance;      // per path of the frame
     kf::DeviceBuffer<kf_hit> primary;       // per path of the frame (debug)
     kf::DeviceBuffer<unsigned long long> stats;
+    kf::DeviceBuffer<uint16_t> path_item;   // batched launches: item of each path of a chunk
     uint32_t chunk_cap = 0, slot_cap = 0;
     uint64_t radiance_cap = 0;
 };
@@ -159,6 +186,8 @@ struct kf_renderer_s {
     kf_denoiser_s* denoiser = nullptr;
     // every denoiser created on this renderer (owned: freed by the renderer's destructor)
     std::vector<kf_denoiser_s*> denoisers;
+    // batched launches (kf_renderer_run_batch)
+    std::unique_ptr<BatchState> batch;
     ~kf_renderer_s();
 };
 
@@ -184,6 +213,10 @@ void camera_ubo(const kf_camera_s* c, kf_camera_ubo* out);
 void scene_light_ubos(const kf_scene_s* s, kf_dir_light_ubo* d, kf_point_lights_ubo* p, kf_active_lights_ubo* a);
 void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s);
 void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp);
+// Brings every scene up to date and (re)builds the batch's concatenated pools if any changed.
+void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes);
+// One frame of every (scene, camera, spp) item in one wavefront (kf_renderer_run_batch).
+void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count);
 
 // global tables
 std::vector<kf_material_gpu> flatten_materials();

@@ -235,15 +235,13 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
 
 } // namespace
 
-// Records the launch sequence of one frame into the renderer stream.
-static void enqueue_frame(kf_renderer_s* r, const SceneDev& sv, const WaveDev& w, uint32_t npix, uint32_t spp,
-                          uint32_t max_depth, uint64_t npaths, uint32_t chunk, int32_t frame_count, kf_camera_s* c,
-                          bool profile) {
+// Records the bounce loop over npaths paths (chunks of `chunk`) into the renderer stream.
+static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* fd, const BatchDev& b,
+                          const WaveDev& w, uint32_t max_depth, uint64_t npaths, uint32_t chunk, bool profile) {
     cudaStream_t st = r->stream;
-    const FrameDev* fd = r->frame_dev.ptr;
     for (uint64_t start = 0; start < npaths; start += chunk) {
         const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, npaths - start);
-        launch_raygen(fd, w, start, n, st);
+        launch_raygen(fd, b, w, start, n, st);
         int cur = 0;
         for (uint32_t depth = 0; depth <= max_depth; ++depth) {
             const bool dyn = r->cfg.traversal == 1;
@@ -252,62 +250,53 @@ static void enqueue_frame(kf_renderer_s* r, const SceneDev& sv, const WaveDev& w
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 3 * sizeof(uint32_t), st));
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[0], st));
             if (dyn)
-                launch_trace_dyn(sv, fd, w, cur, depth, start, false, r->grid_dyn, r->count_traversal, st);
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal, st);
             else
-                launch_extend(sv, fd, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
+                launch_extend(sv, fd, b, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[1], st));
-            launch_shade(sv, fd, w, cur, depth, start, r->grid_shade, st);
+            launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[2], st));
             if (dyn)
-                launch_trace_dyn(sv, fd, w, cur, depth, start, true, r->grid_dyn, r->count_traversal, st);
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, true, r->grid_dyn, r->count_traversal, st);
             else
-                launch_shadow(sv, w, r->grid_extend, r->count_traversal, st);
+                launch_shadow(sv, b, w, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[3], st));
-            launch_gather(sv, fd, w, cur, start, r->grid_shade, st);
+            launch_gather(sv, b, w, cur, start, r->grid_shade, st);
             if (profile) {
                 KF_CUDA_CHECK(cudaEventSynchronize(r->ev[3]));
-                float a = 0, b = 0, d = 0;
+                float a = 0, bb = 0, d = 0;
                 KF_CUDA_CHECK(cudaEventElapsedTime(&a, r->ev[0], r->ev[1]));
-                KF_CUDA_CHECK(cudaEventElapsedTime(&b, r->ev[1], r->ev[2]));
+                KF_CUDA_CHECK(cudaEventElapsedTime(&bb, r->ev[1], r->ev[2]));
                 KF_CUDA_CHECK(cudaEventElapsedTime(&d, r->ev[2], r->ev[3]));
                 r->stats.extend_ms += a;
-                r->stats.shade_ms += b;
+                r->stats.shade_ms += bb;
                 r->stats.shadow_ms += d;
             }
             cur ^= 1;
         }
     }
-    (void)frame_count;
-    launch_resolve(fd, w.radiance, npix, spp, c->accum.ptr, c->sum64.ptr, st);
-    launch_srgb(c->accum.ptr, npix, c->bgra.ptr, st);
 }
 
-void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp) {
-    cudaStream_t st = r->stream;
-    KF_REQUIRE(spp > 0, KF_ERR_INVALID_ARGUMENT, "samples per pixel must be positive");
-    scene_sync_gpu(r, s);
-    ensure_targets(r, c);
-    const uint32_t npix = (uint32_t)c->width * (uint32_t)c->height;
-    const uint64_t npaths = (uint64_t)npix * spp;
-    uint64_t cap = r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24);
-    cap = std::min<uint64_t>(cap, (1ull << 26) - 1);
-    const uint32_t chunk = (uint32_t)std::min<uint64_t>(npaths, cap);
-    const SceneDev& sv = s->gpu.view;
-    ensure_wave(r, chunk, sv.num_slots, npaths);
+// Records the launch sequence of one frame into the renderer stream.
+static void enqueue_frame(kf_renderer_s* r, const SceneDev& sv, const WaveDev& w, uint32_t npix, uint32_t spp,
+                          uint32_t max_depth, uint64_t npaths, uint32_t chunk, kf_camera_s* c, bool profile) {
+    const FrameDev* fd = r->frame_dev.ptr;
+    enqueue_paths(r, sv, fd, BatchDev{nullptr, 0, 0}, w, max_depth, npaths, chunk, profile);
+    launch_resolve(fd, w.radiance, npix, spp, c->accum.ptr, c->sum64.ptr, r->stream);
+    launch_srgb(c->accum.ptr, npix, c->bgra.ptr, r->stream);
+}
 
-    // Context::update (context.cpp:345-349): frame counter for the running mean
-    if (r->cfg.accumulate_frames)
-        ++r->frame_count;
-    else
-        r->frame_count = -1;
-
+// Frame constants of camera c of scene s (push constants: PushConstants.glsl:1-16, filled
+// as Context::update does, context.cpp:345-360).
+static FrameDev make_frame(const kf_renderer_s* r, const kf_scene_s* s, const kf_camera_s* c, uint32_t spp,
+                           int32_t frame_count) {
     FrameDev f{};
     camera_ubo(c, &f.cam);
     f.pc.clear_color[0] = s->clear_color[0];
     f.pc.clear_color[1] = s->clear_color[1];
     f.pc.clear_color[2] = s->clear_color[2];
     f.pc.clear_color[3] = s->clear_color[3];
-    f.pc.frame_count = r->frame_count;
+    f.pc.frame_count = frame_count;
     f.pc.spp = spp;
     f.pc.max_path_depth = r->cfg.path_depth;
     f.pc.use_env_map = s->env_size ? 1u : 0u;
@@ -317,12 +306,39 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
     f.pc.nee_min = r->cfg.nee_min_bounces;
     f.width = (uint32_t)c->width;
     f.height = (uint32_t)c->height;
-    f.npix = npix;
+    f.npix = (uint32_t)c->width * (uint32_t)c->height;
     f.seed = r->cfg.seed;
     f.frame = r->frame_index;
     f.camera_index = 0;
     for (size_t i = 0; i < s->cameras.size(); ++i)
         if (s->cameras[i].get() == c) f.camera_index = (uint32_t)i;
+    return f;
+}
+
+static uint32_t chunk_for(const kf_renderer_s* r, uint64_t npaths) {
+    uint64_t cap = r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24);
+    cap = std::min<uint64_t>(cap, (1ull << 26) - 1);
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(npaths, cap));
+}
+
+void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp) {
+    cudaStream_t st = r->stream;
+    KF_REQUIRE(spp > 0, KF_ERR_INVALID_ARGUMENT, "samples per pixel must be positive");
+    scene_sync_gpu(r, s);
+    ensure_targets(r, c);
+    const uint32_t npix = (uint32_t)c->width * (uint32_t)c->height;
+    const uint64_t npaths = (uint64_t)npix * spp;
+    const uint32_t chunk = chunk_for(r, npaths);
+    const SceneDev& sv = s->gpu.view;
+    ensure_wave(r, chunk, sv.num_slots, npaths);
+
+    // Context::update (context.cpp:345-349): frame counter for the running mean
+    if (r->cfg.accumulate_frames)
+        ++r->frame_count;
+    else
+        r->frame_count = -1;
+
+    const FrameDev f = make_frame(r, s, c, spp, r->frame_count);
     if (r->frame_dev.count == 0) r->frame_dev.resize(1, st);
     KF_CUDA_CHECK(cudaMemcpyAsync(r->frame_dev.ptr, &f, sizeof(f), cudaMemcpyHostToDevice, st));
     KF_CUDA_CHECK(cudaMemsetAsync(c->albedo.ptr, 0, c->albedo.bytes(), st));
@@ -350,7 +366,7 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
             cudaGraph_t g = nullptr;
             KF_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             try {
-                enqueue_frame(r, sv, w, npix, spp, r->cfg.path_depth, npaths, chunk, r->frame_count, c, false);
+                enqueue_frame(r, sv, w, npix, spp, r->cfg.path_depth, npaths, chunk, c, false);
             } catch (...) {
                 cudaStreamEndCapture(st, &g);
                 if (g) cudaGraphDestroy(g);
@@ -363,7 +379,7 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
         }
         KF_CUDA_CHECK(cudaGraphLaunch(r->graph_exec, st));
     } else {
-        enqueue_frame(r, sv, w, npix, spp, r->cfg.path_depth, npaths, chunk, r->frame_count, c, profile);
+        enqueue_frame(r, sv, w, npix, spp, r->cfg.path_depth, npaths, chunk, c, profile);
     }
     if (profile) {
         KF_CUDA_CHECK(cudaEventRecord(f1, st));
@@ -373,9 +389,141 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
         r->stats.frame_ms += ms;
     }
     c->has_frame = true;
+    c->last_path_start = 0;
+    c->last_spp = spp;
     r->stats.frames++;
     r->stats.last_spp = spp;
     r->stats.frame_count = r->frame_count;
+    ++r->frame_index;
+}
+
+// One frame of every item in one wavefront: the items' paths are laid end to end in one
+// path space, the bounce loop runs once over all of them (one launch per kernel per
+// bounce and chunk), then each view is resolved into its own targets. Every view is an
+// independent single frame (frameCount -1, no blending), all with the same frame word.
+void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count) {
+    cudaStream_t st = r->stream;
+    KF_REQUIRE(count > 0, KF_ERR_INVALID_ARGUMENT, "empty batch");
+    KF_REQUIRE(count <= 65535, KF_ERR_LIMIT, "a batch holds at most 65535 views");
+    std::vector<kf_scene_s*> scenes;
+    std::vector<uint32_t> scene_of(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        KF_REQUIRE(items[i].spp > 0, KF_ERR_INVALID_ARGUMENT, "samples per pixel must be positive");
+        auto it = std::find(scenes.begin(), scenes.end(), items[i].scene);
+        if (it == scenes.end()) {
+            scenes.push_back(items[i].scene);
+            it = scenes.end() - 1;
+        }
+        scene_of[i] = (uint32_t)(it - scenes.begin());
+    }
+    batch_sync(r, scenes);
+    BatchState& B = *r->batch;
+    std::vector<ItemDev> hv(count);
+    uint64_t total = 0;
+    uint32_t max_slots = 1;
+    std::vector<uint32_t> inst_base(scenes.size(), 0);
+    for (size_t k = 1; k < scenes.size(); ++k)
+        inst_base[k] = inst_base[k - 1] + (uint32_t)scenes[k - 1]->instances.size();
+    for (uint32_t i = 0; i < count; ++i) {
+        kf_scene_s* s = items[i].scene;
+        kf_camera_s* c = items[i].camera;
+        ensure_targets(r, c);
+        ItemDev& it = hv[i];
+        std::memset(&it, 0, sizeof(it));
+        it.f = make_frame(r, s, c, items[i].spp, -1);
+        it.path_start = total;
+        total += (uint64_t)it.f.npix * items[i].spp;
+        const uint32_t k = scene_of[i];
+        it.root = B.roots[k];
+        const SceneDev& sv = s->gpu.view;
+        it.num_slots = sv.num_slots;
+        std::memcpy(it.slot_group, sv.slot_group, sizeof(it.slot_group));
+        std::memcpy(it.slot_index, sv.slot_index, sizeof(it.slot_index));
+        it.dlight = sv.dlight;
+        it.plights = sv.plights;
+        it.alights = sv.alights;
+        it.env = sv.env;
+        it.env_size = sv.env_size;
+        it.inst_base = inst_base[k];
+        it.albedo = c->albedo.ptr;
+        it.normal = c->normal.ptr;
+        it.depth = c->depth.ptr;
+        max_slots = std::max(max_slots, sv.num_slots);
+    }
+    const uint32_t chunk = chunk_for(r, total);
+    ensure_wave(r, chunk, max_slots, total);
+    if (r->wave.path_item.count < chunk) r->wave.path_item.resize(chunk, st);
+    B.items.resize(count, st);
+    KF_CUDA_CHECK(cudaMemcpyAsync(B.items.ptr, hv.data(), sizeof(ItemDev) * count, cudaMemcpyHostToDevice, st));
+    for (uint32_t i = 0; i < count; ++i) {
+        KF_CUDA_CHECK(cudaMemsetAsync(items[i].camera->albedo.ptr, 0, items[i].camera->albedo.bytes(), st));
+        KF_CUDA_CHECK(cudaMemsetAsync(items[i].camera->normal.ptr, 0, items[i].camera->normal.bytes(), st));
+    }
+    WaveDev w = wave_view(r, items[0].camera);
+    w.path_item = r->wave.path_item.ptr;
+    const BatchDev bd{B.items.ptr, count, 0};
+    auto enqueue = [&](bool profile) {
+        enqueue_paths(r, B.view, nullptr, bd, w, r->cfg.path_depth, total, chunk, profile);
+        for (uint32_t i = 0; i < count; ++i) {
+            kf_camera_s* c = items[i].camera;
+            launch_resolve(&B.items.ptr[i].f, w.radiance + hv[i].path_start, hv[i].f.npix, items[i].spp,
+                           c->accum.ptr, c->sum64.ptr, st);
+            launch_srgb(c->accum.ptr, hv[i].f.npix, c->bgra.ptr, st);
+        }
+    };
+    const bool profile = r->cfg.profile != 0;
+    cudaEvent_t f0 = r->ev[4], f1 = r->ev[5];
+    if (profile) KF_CUDA_CHECK(cudaEventRecord(f0, st));
+    if (r->cfg.use_graph && !profile && !r->count_traversal) {
+        std::string key;
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "%llu|%u|%llu|%u|%p|%p|%p|%u|%u|", (unsigned long long)B.generation, count,
+                      (unsigned long long)total, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)B.items.ptr,
+                      r->cfg.path_depth, r->cfg.russian_roulette | (r->cfg.traversal << 1));
+        key = buf;
+        for (uint32_t i = 0; i < count; ++i) {
+            std::snprintf(buf, sizeof(buf), "%p,%u,%u;", (void*)items[i].camera->accum.ptr, hv[i].f.npix,
+                          items[i].spp);
+            key += buf;
+        }
+        if (!B.graph_exec || B.graph_key != key) {
+            if (B.graph_exec) {
+                cudaGraphExecDestroy(B.graph_exec);
+                B.graph_exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            KF_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue(false);
+            } catch (...) {
+                cudaStreamEndCapture(st, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            KF_CUDA_CHECK(cudaStreamEndCapture(st, &g));
+            KF_CUDA_CHECK(cudaGraphInstantiate(&B.graph_exec, g, 0));
+            cudaGraphDestroy(g);
+            B.graph_key = key;
+        }
+        KF_CUDA_CHECK(cudaGraphLaunch(B.graph_exec, st));
+    } else {
+        enqueue(profile);
+    }
+    if (profile) {
+        KF_CUDA_CHECK(cudaEventRecord(f1, st));
+        KF_CUDA_CHECK(cudaEventSynchronize(f1));
+        float ms = 0;
+        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, f0, f1));
+        r->stats.frame_ms += ms;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        kf_camera_s* c = items[i].camera;
+        c->has_frame = true;
+        c->last_path_start = hv[i].path_start;
+        c->last_spp = items[i].spp;
+    }
+    r->stats.frames += count;
+    r->stats.last_spp = items[count - 1].spp;
     ++r->frame_index;
 }
 

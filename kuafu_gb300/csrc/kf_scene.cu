@@ -427,4 +427,133 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
     r->stats.tlas_nodes = G.tlas_node_count;
 }
 
+// Concatenates the pools of the batch's scenes: vertex, index, material-index and
+// triangle pools are copied as they are (indices are geometry-local, triangle ids too);
+// geometry records, instance records, BLAS / TLAS child links and TLAS leaf entries are
+// rebased by the sizes of the scenes before them.
+void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes) {
+    cudaStream_t st = r->stream;
+    for (kf_scene_s* s : scenes) scene_sync_gpu(r, s);
+    if (!r->batch) r->batch = std::make_unique<BatchState>();
+    BatchState& B = *r->batch;
+    std::vector<uint64_t> gens;
+    for (kf_scene_s* s : scenes) gens.push_back(s->gpu.generation);
+    if (B.scenes == scenes && B.generations == gens) {
+        // lights and slot tables are refreshed by scene_sync_gpu every call; pools are current
+        return;
+    }
+    size_t nv = 0, ni = 0, nt = 0, ng = 0, ninst = 0, nbn = 0, ntn = 0, nti = 0;
+    for (kf_scene_s* s : scenes) {
+        const SceneGpu& G = s->gpu;
+        nv += G.verts.count;
+        ni += G.indices.count;
+        nt += G.matidx.count;
+        ng += s->geometries.size();
+        ninst += s->instances.size();
+        nbn += G.blas_node_count;
+        if (G.tlas_node_count) {
+            ntn += G.tlas_node_count;
+            nti += G.tlas_inst.count;
+        }
+    }
+    KF_REQUIRE(nt < (1ull << 26), KF_ERR_LIMIT, "a batch holds at most 67108863 distinct triangles");
+    KF_REQUIRE(ninst < (1ull << 30), KF_ERR_LIMIT, "too many instances in one batch");
+    B.verts.resize(std::max<size_t>(nv, 1), st);
+    B.indices.resize(std::max<size_t>(ni, 1), st);
+    B.matidx.resize(std::max<size_t>(nt, 1), st);
+    B.tris.resize(std::max<size_t>(nt, 1), st);
+    B.geom.resize(std::max<size_t>(ng, 1), st);
+    B.inst.resize(std::max<size_t>(ninst, 1), st);
+    B.blas_nodes.resize(std::max<size_t>(nbn, 1), st);
+    B.tlas_nodes.resize(std::max<size_t>(ntn, 1), st);
+    B.tlas_inst.resize(std::max<size_t>(nti, 1), st);
+    B.roots.assign(scenes.size(), kNoRoot);
+    size_t ov = 0, oi = 0, ot = 0, og = 0, oinst = 0, obn = 0, otn = 0, oti = 0;
+    std::vector<uint4> geom;
+    std::vector<InstanceRec> inst;
+    std::vector<uint32_t> tinst;
+    for (size_t k = 0; k < scenes.size(); ++k) {
+        kf_scene_s* s = scenes[k];
+        const SceneGpu& G = s->gpu;
+        auto copy = [&](void* dst, const void* src, size_t bytes) {
+            if (bytes) KF_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+        };
+        copy(B.verts.ptr + ov, G.verts.ptr, G.verts.count * sizeof(float4));
+        copy(B.indices.ptr + oi, G.indices.ptr, G.indices.count * sizeof(uint32_t));
+        const size_t sct = G.matidx.count;
+        copy(B.matidx.ptr + ot, G.matidx.ptr, sct * sizeof(uint32_t));
+        copy(B.tris.ptr + ot, G.tris.ptr, sct * sizeof(Tri));
+        // geometry records: vertex offsets count vertices (3 float4 each)
+        for (size_t gi = 0; gi < s->geometries.size(); ++gi) {
+            const kf_geometry_s* g = s->geometries[gi];
+            const uint32_t flags = (g->opaque ? 1u : 0u) | (g->hide_render ? 2u : 0u);
+            geom.push_back(make_uint4(G.vert_offset[gi] + (uint32_t)(ov / 3), G.tri_offset[gi] + (uint32_t)ot,
+                                      (uint32_t)(g->indices.size() / 3), flags));
+        }
+        const size_t sn = s->instances.size();
+        if (sn) {
+            std::vector<InstanceRec> recs(sn);
+            KF_CUDA_CHECK(cudaMemcpyAsync(recs.data(), G.inst.ptr, sn * sizeof(InstanceRec), cudaMemcpyDeviceToHost, st));
+            KF_CUDA_CHECK(cudaStreamSynchronize(st));
+            for (InstanceRec& rc : recs) {
+                rc.blas_root += (uint32_t)obn;
+                rc.geometry += (uint32_t)og;
+                inst.push_back(rc);
+            }
+        }
+        if (G.blas_node_count) {
+            k_rebase<<<(G.blas_node_count + 127) / 128, 128, 0, st>>>(G.blas_nodes.ptr, G.blas_node_count,
+                                                                      (uint32_t)obn, (uint32_t)ot,
+                                                                      B.blas_nodes.ptr + obn);
+            KF_CUDA_CHECK(cudaGetLastError());
+        }
+        if (G.tlas_node_count) {
+            k_rebase<<<(G.tlas_node_count + 127) / 128, 128, 0, st>>>(G.tlas_nodes.ptr, G.tlas_node_count,
+                                                                      (uint32_t)otn, (uint32_t)oti,
+                                                                      B.tlas_nodes.ptr + otn);
+            KF_CUDA_CHECK(cudaGetLastError());
+            std::vector<uint32_t> ti(G.tlas_inst.count);
+            KF_CUDA_CHECK(cudaMemcpyAsync(ti.data(), G.tlas_inst.ptr, ti.size() * 4, cudaMemcpyDeviceToHost, st));
+            KF_CUDA_CHECK(cudaStreamSynchronize(st));
+            for (uint32_t v : ti) tinst.push_back(v + (uint32_t)oinst);
+            B.roots[k] = (uint32_t)otn;
+            otn += G.tlas_node_count;
+            oti += ti.size();
+        }
+        ov += G.verts.count;
+        oi += G.indices.count;
+        ot += sct;
+        og += s->geometries.size();
+        oinst += sn;
+        obn += G.blas_node_count;
+    }
+    if (!geom.empty()) B.geom.upload(geom.data(), geom.size(), st);
+    if (!inst.empty()) B.inst.upload(inst.data(), inst.size(), st);
+    if (!tinst.empty()) B.tlas_inst.upload(tinst.data(), tinst.size(), st);
+    KF_CUDA_CHECK(cudaStreamSynchronize(st));
+    const SceneDev& v0 = scenes.front()->gpu.view;
+    SceneDev& v = B.view;
+    v = v0; // materials, textures, sRGB table: process-global, identical in every scene
+    v.verts = B.verts.ptr;
+    v.indices = B.indices.ptr;
+    v.matidx = B.matidx.ptr;
+    v.geom = B.geom.ptr;
+    v.inst = B.inst.ptr;
+    v.blas_nodes = B.blas_nodes.ptr;
+    v.tris = B.tris.ptr;
+    v.tlas_nodes = B.tlas_nodes.ptr;
+    v.tlas_inst = B.tlas_inst.ptr;
+    v.num_instances = (uint32_t)ninst;
+    v.has_tlas = 0;        // each view starts at its own root
+    v.num_slots = 0;       // each view has its own light slots
+    v.dlight = nullptr;
+    v.plights = nullptr;
+    v.alights = nullptr;
+    v.env = nullptr;
+    v.env_size = 0;
+    B.scenes = scenes;
+    B.generations = gens;
+    ++B.generation;
+}
+
 } // namespace kf

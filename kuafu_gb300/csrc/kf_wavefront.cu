@@ -91,8 +91,9 @@ template <bool SHADOW, bool COUNT> struct Tracer {
     HitOut h;
     TraceCounters cnt;
 
-    __device__ __forceinline__ void init(const SceneDev& s, float ox, float oy, float oz, float dx, float dy,
-                                         float dz, float tmin_, float tmax_) {
+    // root: the TLAS root node of the ray's scene (kNoRoot: the ray hits nothing)
+    __device__ __forceinline__ void init(uint32_t root, float ox, float oy, float oz, float dx, float dy, float dz,
+                                         float tmin_, float tmax_) {
         h.inst = kMiss;
         h.t = h.u = h.v = 0.0f;
         h.prim = 0;
@@ -101,7 +102,7 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         prep_ray(wr);
         r = wr;
         sp = 0;
-        if (s.has_tlas) stack.put(sp++, 0);
+        if (root != kNoRoot) stack.put(sp++, root);
         in_blas = false;
         cur_inst = cur_geom = 0;
         cur_opaque = true;
@@ -215,11 +216,12 @@ template <bool SHADOW, bool COUNT> struct Tracer {
 
 // smem: the block's shared stack area (kSmemStack * kThreadsTrace words).
 template <bool SHADOW, bool COUNT>
-__device__ bool trace(const SceneDev& s, uint32_t* smem, float ox, float oy, float oz, float dx, float dy, float dz,
-                      float tmin, float tmax, HitOut& h, TraceCounters& cnt, AnyHitCtx* ah = nullptr) {
+__device__ bool trace(const SceneDev& s, uint32_t root, uint32_t* smem, float ox, float oy, float oz, float dx,
+                      float dy, float dz, float tmin, float tmax, HitOut& h, TraceCounters& cnt,
+                      AnyHitCtx* ah = nullptr) {
     Tracer<SHADOW, COUNT> t;
     t.stack.sm = smem + threadIdx.x;
-    t.init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
+    t.init(root, ox, oy, oz, dx, dy, dz, tmin, tmax);
     t.cnt = cnt;
 #pragma unroll 1
     while (!t.step(s, ah)) {
@@ -254,15 +256,62 @@ __device__ __forceinline__ void mat4_mul(const float* m, const float v[4], float
     for (int r = 0; r < 4; ++r) out[r] = m[0 * 4 + r] * v[0] + m[1 * 4 + r] * v[1] + m[2 * 4 + r] * v[2] + m[3 * 4 + r] * v[3];
 }
 
+// Batched launches: the item of global path G (items sorted by path_start, item 0 starts at 0).
+__device__ __forceinline__ uint32_t find_item(const BatchDev& b, uint64_t G) {
+    uint32_t lo = 0, hi = b.num_items;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.items[mid].path_start <= G) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The view a path belongs to: single-view frames use the scene's own TLAS root; batched
+// ones the root of the path's item (paths carry their item in w.path_item).
+template <bool BATCH> struct View {
+    const FrameDev* f;
+    const ItemDev* it;
+    uint64_t g; // path index within the view
+};
+template <bool BATCH>
+__device__ __forceinline__ View<BATCH> view_of(const FrameDev* fp, const BatchDev& b, const WaveDev& w,
+                                               uint64_t chunk_start, uint32_t p) {
+    View<BATCH> v;
+    if (BATCH) {
+        v.it = b.items + w.path_item[p];
+        v.f = &v.it->f;
+        v.g = chunk_start + p - v.it->path_start;
+    } else {
+        v.it = nullptr;
+        v.f = fp;
+        v.g = chunk_start + p;
+    }
+    return v;
+}
+template <bool BATCH> __device__ __forceinline__ uint32_t root_of(const SceneDev& s, const View<BATCH>& v) {
+    if (BATCH) return v.it->root;
+    return s.has_tlas ? 0u : kNoRoot;
+}
+
 // ---------------------------------------------------------------------------
 // Ray generation (PathTrace.rgen:30-75).
 // ---------------------------------------------------------------------------
-__global__ void k_raygen(const FrameDev* __restrict__ fp, WaveDev w, uint64_t chunk_start, uint32_t chunk_n) {
+template <bool BATCH>
+__global__ void k_raygen(const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, uint64_t chunk_start,
+                         uint32_t chunk_n) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p == 0) w.counters[0] = chunk_n;
     if (p >= chunk_n) return;
-    const FrameDev& f = *fp;
-    const uint64_t g = chunk_start + p;
+    uint64_t g = chunk_start + p;
+    const FrameDev* fsel = fp;
+    if (BATCH) {
+        const uint32_t item = find_item(b, g);
+        w.path_item[p] = (uint16_t)item;
+        fsel = &b.items[item].f;
+        g -= b.items[item].path_start;
+    }
+    const FrameDev& f = *fsel;
     const uint32_t sample = (uint32_t)(g / f.npix);
     const uint32_t pix = (uint32_t)(g % f.npix);
     const uint32_t px = pix % f.width, py = pix / f.width;
@@ -310,15 +359,15 @@ __global__ void k_raygen(const FrameDev* __restrict__ fp, WaveDev w, uint64_t ch
     w.q_o[0][p] = make_float4(origin[0], origin[1], origin[2], __uint_as_float(p));
     w.q_d[0][p] = make_float4(dir[0], dir[1], dir[2], 0.0f);
     w.weight[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    w.radiance[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.radiance[chunk_start + p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // ---------------------------------------------------------------------------
 // Closest-hit extension (traceRayEXT with tMin 0.001, tMax 10000).
 // ---------------------------------------------------------------------------
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
-                                                uint32_t depth, uint64_t chunk_start) {
+template <bool COUNT, bool BATCH>
+__global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+                                                int cur, uint32_t depth, uint64_t chunk_start) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = w.counters[cur];
     const float4* __restrict__ qo = w.q_o[cur];
@@ -328,20 +377,23 @@ __global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __re
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const float4 o = qo[i], d = qd[i];
         HitOut h;
-        const uint64_t g = chunk_start + __float_as_uint(o.w);
-        const uint32_t npix = fp->npix;
-        const PathKey pk{make_uint2(fp->seed ^ (uint32_t)(g % npix), fp->camera_index), (uint32_t)(g / npix),
-                         fp->frame};
+        const View<BATCH> v = view_of<BATCH>(fp, b, w, chunk_start, __float_as_uint(o.w));
+        const uint64_t g = v.g;
+        const uint32_t npix = v.f->npix;
+        const PathKey pk{make_uint2(v.f->seed ^ (uint32_t)(g % npix), v.f->camera_index), (uint32_t)(g / npix),
+                         v.f->frame};
         AnyHitCtx ah;
         ah.pk = &pk;
         ah.st.init(depth, KF_RNG_ANYHIT);
-        trace<false, COUNT>(s, s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h, cnt, &ah);
+        trace<false, COUNT>(s, root_of<BATCH>(s, v), s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h,
+                            cnt, &ah);
         w.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
         w.hit_prim[i] = h.prim;
         if (depth == 0 && w.primary) {
             const uint32_t p = __float_as_uint(o.w);
             kf_hit ph;
-            ph.t = h.t; ph.u = h.u; ph.v = h.v; ph.instance = h.inst; ph.prim = h.prim;
+            ph.t = h.t; ph.u = h.u; ph.v = h.v; ph.prim = h.prim;
+            ph.instance = (BATCH && h.inst != kMiss) ? h.inst - v.it->inst_base : h.inst; // scene-local id
             ph.pad[0] = ph.pad[1] = ph.pad[2] = 0;
             w.primary[chunk_start + p] = ph;
         }
@@ -424,8 +476,8 @@ __device__ __forceinline__ v3 uniformSphereSampling(Stream& st, const PathKey& p
 
 // Environment lookup of PathTrace.rmiss:14-29: texture(environmentMap, vec3(-d.y, d.z, -d.x)).
 // Face selection by the major axis and face coordinates (sc, tc) of the Vulkan / GL cube
-// rules; bilinear within the face, clamp to edge.
-__device__ v3 env_lookup(const SceneDev& s, v3 d) {
+// rules; bilinear within the face, clamp to edge. env: 6 faces of env_size^2 texels.
+__device__ v3 env_lookup(const float4* env, uint32_t env_size, v3 d) {
     const float rx = -d.y, ry = d.z, rz = -d.x;
     const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
     uint32_t face;
@@ -446,7 +498,7 @@ __device__ v3 env_lookup(const SceneDev& s, v3 d) {
         sc = rz >= 0.0f ? rx : -rx;
         tc = -ry;
     }
-    const uint32_t n = s.env_size;
+    const uint32_t n = env_size;
     const float fs = 0.5f * (sc / ma + 1.0f), ft = 0.5f * (tc / ma + 1.0f);
     const float x = fs * (float)n - 0.5f, y = ft * (float)n - 0.5f;
     const float fx0 = floorf(x), fy0 = floorf(y);
@@ -454,7 +506,7 @@ __device__ v3 env_lookup(const SceneDev& s, v3 d) {
     const int ix = (int)fx0, iy = (int)fy0, hi = (int)n - 1;
     const uint32_t x0 = (uint32_t)min(max(ix, 0), hi), x1 = (uint32_t)min(max(ix + 1, 0), hi);
     const uint32_t y0 = (uint32_t)min(max(iy, 0), hi), y1 = (uint32_t)min(max(iy + 1, 0), hi);
-    const float4* fp = s.env + (size_t)face * n * n;
+    const float4* fp = env + (size_t)face * n * n;
     const float4 t00 = __ldg(fp + (size_t)y0 * n + x0), t10 = __ldg(fp + (size_t)y0 * n + x1);
     const float4 t01 = __ldg(fp + (size_t)y1 * n + x0), t11 = __ldg(fp + (size_t)y1 * n + x1);
     const v3 top = mk(t00.x, t00.y, t00.z) * (1.0f - wx) + mk(t10.x, t10.y, t10.z) * wx;
@@ -548,16 +600,37 @@ __device__ v3 calcDirectContribution(Stream& st, const PathKey& pk, v3 L, v3 V, 
     return lightEmission * weight;
 }
 
+// Light slots of a view: the scene's own (single-view frame) or its item's (batched).
+struct SceneLights {
+    const SceneDev& s;
+    __device__ __forceinline__ uint32_t num() const { return s.num_slots; }
+    __device__ __forceinline__ uint32_t group(uint32_t j) const { return s.slot_group[j]; }
+    __device__ __forceinline__ uint32_t index(uint32_t j) const { return s.slot_index[j]; }
+    __device__ __forceinline__ const kf_dir_light_ubo* dlight() const { return s.dlight; }
+    __device__ __forceinline__ const kf_point_lights_ubo* plights() const { return s.plights; }
+    __device__ __forceinline__ const kf_active_lights_ubo* alights() const { return s.alights; }
+};
+struct ItemLights {
+    const ItemDev* it;
+    __device__ __forceinline__ uint32_t num() const { return it->num_slots; }
+    __device__ __forceinline__ uint32_t group(uint32_t j) const { return it->slot_group[j]; }
+    __device__ __forceinline__ uint32_t index(uint32_t j) const { return it->slot_index[j]; }
+    __device__ __forceinline__ const kf_dir_light_ubo* dlight() const { return it->dlight; }
+    __device__ __forceinline__ const kf_point_lights_ubo* plights() const { return it->plights; }
+    __device__ __forceinline__ const kf_active_lights_ubo* alights() const { return it->alights; }
+};
+
 // One light slot's sample: returns true if a shadow ray is needed (NdotL > 0 and a
 // non-zero contribution), with its direction, length and contribution.
-__device__ bool light_sample(const SceneDev& s, uint32_t slot, uint32_t depth, const PathKey& pk, v3 worldPos, v3 N,
-                             v3 V, const Shading& sh, v3& Lout, float& tmax, v3& contrib) {
-    const uint32_t group = s.slot_group[slot], li = s.slot_index[slot];
+template <class LS>
+__device__ bool light_sample(const SceneDev& s, const LS& ls, uint32_t slot, uint32_t depth, const PathKey& pk,
+                             v3 worldPos, v3 N, v3 V, const Shading& sh, v3& Lout, float& tmax, v3& contrib) {
+    const uint32_t group = ls.group(slot), li = ls.index(slot);
     Stream st;
     v3 L, lightEmission;
     float maxDist;
     if (group == 0) { // traceDirectionalLight (rchit:204-223)
-        const kf_dir_light_ubo* dl = s.dlight;
+        const kf_dir_light_ubo* dl = ls.dlight();
         st.init(depth, KF_RNG_DIRLIGHT);
         lightEmission = ld3(dl->rgbs) * dl->rgbs[3];
         if (lightEmission == splat(0.0f)) return false;
@@ -568,7 +641,7 @@ __device__ bool light_sample(const SceneDev& s, uint32_t slot, uint32_t depth, c
         }
         maxDist = KF_DIR_LIGHT_TMAX;
     } else if (group == 1) { // tracePointLights (rchit:227-258)
-        const kf_point_lights_ubo* pl = s.plights;
+        const kf_point_lights_ubo* pl = ls.plights();
         st.init(depth, KF_RNG_POINT0 + li);
         if (!(pl->rgbs[li][3] > 0.0f)) return false;
         const float lum = length(ld3(pl->rgbs[li]) * pl->rgbs[li][3]);
@@ -584,7 +657,7 @@ __device__ bool light_sample(const SceneDev& s, uint32_t slot, uint32_t depth, c
         lightEmission = ld3(pl->rgbs[li]) * pl->rgbs[li][3] / d / d;
         maxDist = d;
     } else { // traceActiveLights (rchit:262-316)
-        const kf_active_lights_ubo* al = s.alights;
+        const kf_active_lights_ubo* al = ls.alights();
         st.init(depth, KF_RNG_ACTIVE0 + li);
         if (!(al->front[li][3] > 0.0f)) return false;
         const float lum = length(ld3(al->rgbs[li]) * al->rgbs[li][3]);
@@ -639,9 +712,9 @@ __device__ bool light_sample(const SceneDev& s, uint32_t slot, uint32_t depth, c
 // ---------------------------------------------------------------------------
 // Shade: miss / emission / PrincipledBSDF (rchit:322-468), light samples, RR.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
-                                               uint32_t depth, uint64_t chunk_start) {
-    const FrameDev& f = *fp;
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+                                               int cur, uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[cur];
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31;
@@ -659,13 +732,21 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
         sh.f = 1.0f; sh.a2 = 0.0f;
         sh.diffuseColor = sh.specularColor = sh.transmissionColor = splat(0.0f);
         sh.isInside = false;
+        View<BATCH> vw{fp, nullptr, 0};
         if (valid) {
             const float4 qo = w.q_o[cur][i], qd = w.q_d[cur][i];
             p = __float_as_uint(qo.w);
-            g = chunk_start + p;
-            const uint32_t sample = (uint32_t)(g / f.npix);
-            const uint32_t pix = (uint32_t)(g % f.npix);
+            g = chunk_start + p; // radiance index (the batch's path space)
+            vw = view_of<BATCH>(fp, b, w, chunk_start, p);
+            const FrameDev& f = *vw.f;
+            const uint32_t sample = (uint32_t)(vw.g / f.npix);
+            const uint32_t pix = (uint32_t)(vw.g % f.npix);
             pk = PathKey{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
+            const float4* env = BATCH ? vw.it->env : s.env;
+            const uint32_t env_size = BATCH ? vw.it->env_size : s.env_size;
+            float4* aov_albedo = BATCH ? vw.it->albedo : w.albedo;
+            float4* aov_normal = BATCH ? vw.it->normal : w.normal;
+            float* aov_depth = BATCH ? vw.it->depth : w.depth;
             const float4 hv = w.hit[i];
             const uint32_t inst = __float_as_uint(hv.w);
             const float4 w4 = w.weight[p];
@@ -675,8 +756,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
             const v3 rayD = mk(qd.x, qd.y, qd.z);
             if (inst == kMiss) {
                 // PathTrace.rmiss:12-31: environment map, else clear colour
-                const v3 emission = (f.pc.use_env_map && s.env) ? env_lookup(s, rayD)
-                                                                 : ld3(f.pc.clear_color) * f.pc.clear_color[3];
+                const v3 emission = (f.pc.use_env_map && env) ? env_lookup(env, env_size, rayD)
+                                                               : ld3(f.pc.clear_color) * f.pc.clear_color[3];
                 color = color + emission * wold;
                 w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
             } else {
@@ -811,8 +892,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
                     sh.isInside = isInside;
                     // AOVs of sample 0, first bounce (rgen:114-117)
                     if (depth == 0 && sample == 0) {
-                        w.albedo[pix] = make_float4(baseColor.x, baseColor.y, baseColor.z, 1.0f);
-                        w.normal[pix] = make_float4(N.x, N.y, N.z, 1.0f);
+                        aov_albedo[pix] = make_float4(baseColor.x, baseColor.y, baseColor.z, 1.0f);
+                        aov_normal[pix] = make_float4(N.x, N.y, N.z, 1.0f);
                     }
                     // rgen:110  weight *= ray.weight
                     wnew = wold * weight;
@@ -834,14 +915,21 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
                     }
                 }
             }
-            if (depth == 0 && sample == 0) w.depth[pix] = inst == kMiss ? 0.0f : hv.x;
+            if (depth == 0 && sample == 0) aov_depth[pix] = inst == kMiss ? 0.0f : hv.x;
         }
         // light slots: one warp-uniform loop, one ballot per slot
         uint64_t req = 0;
-        for (uint32_t j = 0; j < s.num_slots; ++j) {
+        const uint32_t nslots =
+            BATCH ? __reduce_max_sync(kFull, valid ? vw.it->num_slots : 0u) : s.num_slots;
+        for (uint32_t j = 0; j < nslots; ++j) {
             v3 Ls = splat(0.0f), c = splat(0.0f);
             float tmax = 0.0f;
-            const bool emit = is_mat && light_sample(s, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
+            bool emit;
+            if (BATCH)
+                emit = is_mat && j < vw.it->num_slots &&
+                       light_sample(s, ItemLights{vw.it}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
+            else
+                emit = is_mat && light_sample(s, SceneLights{s}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
             const uint32_t pos = warp_append(emit, &w.counters[2]);
             if (emit) {
                 w.sq_o[pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
@@ -867,21 +955,21 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __res
 // ---------------------------------------------------------------------------
 // Shadow rays: any hit in [0.001, tmax] (rchit:175-200, PathTraceShadow.rmiss).
 // ---------------------------------------------------------------------------
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_shadow(SceneDev s, WaveDev w) {
+template <bool COUNT, bool BATCH>
+__global__ void __launch_bounds__(128) k_shadow(SceneDev s, BatchDev b, WaveDev w) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = w.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[2], (unsigned long long)count);
     TraceCounters cnt{0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const float4 o = w.sq_o[i], d = w.sq_d[i];
+        const uint32_t tag = __float_as_uint(d.w);
+        const uint32_t slot = tag >> 26, p = tag & ((1u << 26) - 1u);
+        const uint32_t root = BATCH ? b.items[w.path_item[p]].root : (s.has_tlas ? 0u : kNoRoot);
         HitOut h;
-        const bool occluded = trace<true, COUNT>(s, s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w, h, cnt);
-        if (!occluded) {
-            const uint32_t tag = __float_as_uint(d.w);
-            const uint32_t slot = tag >> 26, p = tag & ((1u << 26) - 1u);
-            w.vis[(size_t)slot * w.chunk_cap + p] = 1;
-        }
+        const bool occluded =
+            trace<true, COUNT>(s, root, s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w, h, cnt);
+        if (!occluded) w.vis[(size_t)slot * w.chunk_cap + p] = 1;
     }
     if (COUNT) {
         atomicAdd(&w.stats[6], (unsigned long long)cnt.nodes);
@@ -900,16 +988,16 @@ __global__ void __launch_bounds__(128) k_shadow(SceneDev s, WaveDev w) {
 constexpr uint32_t kRefillBelow = 24;
 constexpr int kStepsPerRefill = 8;
 
-template <bool SHADOW, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur,
-                                                   uint32_t depth, uint64_t chunk_start) {
+template <bool SHADOW, bool COUNT, bool BATCH>
+__global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b,
+                                                   WaveDev w, int cur, uint32_t depth, uint64_t chunk_start) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = SHADOW ? w.counters[2] : w.counters[cur];
     uint32_t* fetch = w.counters + (SHADOW ? 4 : 3);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         atomicAdd(&w.stats[SHADOW ? 2 : (depth == 0 ? 0 : 1)], (unsigned long long)count);
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t npix = fp->npix;
+    const uint32_t single_root = s.has_tlas ? 0u : kNoRoot;
     Tracer<SHADOW, COUNT> t;
     t.stack.sm = s_stack + threadIdx.x;
     t.cnt = TraceCounters{0, 0, 0};
@@ -935,14 +1023,17 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* _
                     idx = j;
                     if (SHADOW) {
                         const float4 o = w.sq_o[j], d = w.sq_d[j];
-                        t.init(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w);
+                        const uint32_t p = __float_as_uint(d.w) & ((1u << 26) - 1u);
+                        const uint32_t root = BATCH ? b.items[w.path_item[p]].root : single_root;
+                        t.init(root, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w);
                     } else {
                         const float4 o = w.q_o[cur][j], d = w.q_d[cur][j];
-                        const uint64_t g = chunk_start + __float_as_uint(o.w);
-                        pk = PathKey{make_uint2(fp->seed ^ (uint32_t)(g % npix), fp->camera_index),
-                                     (uint32_t)(g / npix), fp->frame};
+                        const View<BATCH> v = view_of<BATCH>(fp, b, w, chunk_start, __float_as_uint(o.w));
+                        const uint32_t npix = v.f->npix;
+                        pk = PathKey{make_uint2(v.f->seed ^ (uint32_t)(v.g % npix), v.f->camera_index),
+                                     (uint32_t)(v.g / npix), v.f->frame};
                         ah.st.init(depth, KF_RNG_ANYHIT);
-                        t.init(s, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX);
+                        t.init(BATCH ? v.it->root : single_root, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX);
                     }
                     active = true;
                 }
@@ -966,7 +1057,10 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* _
                     if (depth == 0 && w.primary) {
                         const uint32_t p = __float_as_uint(w.q_o[cur][idx].w);
                         kf_hit ph;
-                        ph.t = t.h.t; ph.u = t.h.u; ph.v = t.h.v; ph.instance = t.h.inst; ph.prim = t.h.prim;
+                        ph.t = t.h.t; ph.u = t.h.u; ph.v = t.h.v; ph.prim = t.h.prim;
+                        ph.instance = (BATCH && t.h.inst != kMiss)
+                                          ? t.h.inst - b.items[w.path_item[p]].inst_base // scene-local id
+                                          : t.h.inst;
                         ph.pad[0] = ph.pad[1] = ph.pad[2] = 0;
                         w.primary[chunk_start + p] = ph;
                     }
@@ -986,12 +1080,14 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* _
 // Gather: shadow_color = traceDirectionalLight + tracePointLights + traceActiveLights
 // (rchit:457-460), color += shadow_color * weight (rgen:111).
 // ---------------------------------------------------------------------------
-__global__ void k_gather(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w, int cur, uint64_t chunk_start) {
+template <bool BATCH>
+__global__ void k_gather(SceneDev s, BatchDev b, WaveDev w, int cur, uint64_t chunk_start) {
     const uint32_t count = w.counters[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t p = __float_as_uint(w.q_o[cur][i].w);
         uint64_t req = w.req[p];
         if (!req) continue;
+        const uint8_t* slot_group = BATCH ? b.items[w.path_item[p]].slot_group : nullptr;
         v3 D = splat(0.0f), P = splat(0.0f), A = splat(0.0f);
         while (req) {
             const uint32_t j = __ffsll((long long)req) - 1;
@@ -999,7 +1095,7 @@ __global__ void k_gather(SceneDev s, const FrameDev* __restrict__ fp, WaveDev w,
             if (!w.vis[(size_t)j * w.chunk_cap + p]) continue;
             const float4 c4 = w.contrib[(size_t)j * w.chunk_cap + p];
             const v3 c = mk(c4.x, c4.y, c4.z);
-            const uint32_t grp = s.slot_group[j];
+            const uint32_t grp = BATCH ? slot_group[j] : s.slot_group[j];
             if (grp == 0) D = c;
             else if (grp == 1) P = P + c;
             else A = A + c;
@@ -1095,56 +1191,93 @@ __global__ void k_relmse_final(const double* partial, uint32_t blocks, uint64_t 
 
 } // namespace
 
-void launch_raygen(const FrameDev* f, const WaveDev& w, uint64_t chunk_start, uint32_t chunk_n, cudaStream_t st) {
-    k_raygen<<<(chunk_n + 255) / 256, 256, 0, st>>>(f, w, chunk_start, chunk_n);
-    KF_CUDA_CHECK(cudaGetLastError());
-}
-void launch_extend(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                   uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st) {
-    if (count_mode)
-        k_extend<true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+void launch_raygen(const FrameDev* f, const BatchDev& b, const WaveDev& w, uint64_t chunk_start, uint32_t chunk_n,
+                   cudaStream_t st) {
+    const unsigned grid = (chunk_n + 255) / 256;
+    if (b.items)
+        k_raygen<true><<<grid, 256, 0, st>>>(f, b, w, chunk_start, chunk_n);
     else
-        k_extend<false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+        k_raygen<false><<<grid, 256, 0, st>>>(f, b, w, chunk_start, chunk_n);
     KF_CUDA_CHECK(cudaGetLastError());
 }
-void launch_shade(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                  uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
-    k_shade<<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
-    KF_CUDA_CHECK(cudaGetLastError());
-}
-void launch_shadow(const SceneDev& s, const WaveDev& w, uint32_t grid, bool count_mode, cudaStream_t st) {
-    if (count_mode)
-        k_shadow<true><<<grid, 128, 0, st>>>(s, w);
-    else
-        k_shadow<false><<<grid, 128, 0, st>>>(s, w);
-    KF_CUDA_CHECK(cudaGetLastError());
-}
-void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                      uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode, cudaStream_t st) {
-    if (shadow) {
+void launch_extend(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                   uint32_t depth, uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st) {
+    if (b.items) {
         if (count_mode)
-            k_trace_dyn<true, true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+            k_extend<true, true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
         else
-            k_trace_dyn<true, false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+            k_extend<false, true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     } else {
         if (count_mode)
-            k_trace_dyn<false, true><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+            k_extend<true, false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
         else
-            k_trace_dyn<false, false><<<grid, 128, 0, st>>>(s, f, w, cur, depth, chunk_start);
+            k_extend<false, false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    }
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                  uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
+    if (b.items)
+        k_shade<true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    else
+        k_shade<false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
+                   cudaStream_t st) {
+    if (b.items) {
+        if (count_mode)
+            k_shadow<true, true><<<grid, 128, 0, st>>>(s, b, w);
+        else
+            k_shadow<false, true><<<grid, 128, 0, st>>>(s, b, w);
+    } else {
+        if (count_mode)
+            k_shadow<true, false><<<grid, 128, 0, st>>>(s, b, w);
+        else
+            k_shadow<false, false><<<grid, 128, 0, st>>>(s, b, w);
     }
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
-uint32_t trace_dyn_blocks_per_sm() {
-    int a = 0, b = 0;
-    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<false, false>, 128, 0));
-    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_dyn<true, false>, 128, 0));
-    return (uint32_t)std::max(1, std::min(a, b));
+template <bool BATCH>
+static void trace_dyn_dispatch(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                               uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
+                               cudaStream_t st) {
+    if (shadow) {
+        if (count_mode)
+            k_trace_dyn<true, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        else
+            k_trace_dyn<true, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    } else {
+        if (count_mode)
+            k_trace_dyn<false, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        else
+            k_trace_dyn<false, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    }
+}
+void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                      uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
+                      cudaStream_t st) {
+    if (b.items)
+        trace_dyn_dispatch<true>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, st);
+    else
+        trace_dyn_dispatch<false>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, st);
+    KF_CUDA_CHECK(cudaGetLastError());
 }
 
-void launch_gather(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint64_t chunk_start,
+uint32_t trace_dyn_blocks_per_sm() {
+    int a = 0, c = 0;
+    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<false, false, false>, 128, 0));
+    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_trace_dyn<true, false, false>, 128, 0));
+    return (uint32_t)std::max(1, std::min(a, c));
+}
+
+void launch_gather(const SceneDev& s, const BatchDev& b, const WaveDev& w, int cur, uint64_t chunk_start,
                    uint32_t grid, cudaStream_t st) {
-    k_gather<<<grid, 256, 0, st>>>(s, f, w, cur, chunk_start);
+    if (b.items)
+        k_gather<true><<<grid, 256, 0, st>>>(s, b, w, cur, chunk_start);
+    else
+        k_gather<false><<<grid, 256, 0, st>>>(s, b, w, cur, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_resolve(const FrameDev* f, const float4* radiance, uint32_t npix, uint32_t spp, float4* accum,

@@ -47,6 +47,37 @@ struct FrameDev {
     uint32_t frame, camera_index, pad0, pad1;
 };
 
+constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
+
+// One view of a batched launch: its frame constants, where its paths start in the
+// batch's path space, and what of its scene the kernels need beyond the shared
+// (concatenated) geometry / BVH pools: TLAS root, light slots, environment, AOVs.
+struct ItemDev {
+    FrameDev f;
+    uint64_t path_start;
+    uint32_t root;            // TLAS root node in the batch's node pool (kNoRoot: nothing to hit)
+    uint32_t num_slots;
+    uint8_t slot_group[kMaxLightSlots];
+    uint8_t slot_index[kMaxLightSlots];
+    uint16_t pad;
+    const kf_dir_light_ubo* dlight;
+    const kf_point_lights_ubo* plights;
+    const kf_active_lights_ubo* alights;
+    const float4* env;
+    uint32_t env_size;
+    uint32_t inst_base;       // first instance of the item's scene in the batch's instance pool
+    float4* albedo;
+    float4* normal;
+    float* depth;
+};
+
+// Batch description handed to the kernels (items == nullptr: a single-view frame).
+struct BatchDev {
+    const ItemDev* items;
+    uint32_t num_items;
+    uint32_t pad;
+};
+
 // Per-chunk wavefront state.
 struct WaveDev {
     float4* q_o[2];       // ray queue: origin.xyz + path id bits
@@ -67,21 +98,28 @@ struct WaveDev {
     float4* normal;
     float* depth;
     unsigned long long* stats; // [0] primary, [1] extension, [2] shadow, [3] nodes, [4] tris, [5] inst
+    uint16_t* path_item;       // batched launch: item of each path of the chunk
     uint32_t chunk_cap;
 };
 
-void launch_raygen(const FrameDev* f, const WaveDev& w, uint64_t chunk_start, uint32_t chunk_n, cudaStream_t st);
-void launch_extend(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                   uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st);
-void launch_shade(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                  uint64_t chunk_start, uint32_t grid, cudaStream_t st);
-void launch_shadow(const SceneDev& s, const WaveDev& w, uint32_t grid, bool count_mode, cudaStream_t st);
+// Every launcher takes the batch description b: b.items == nullptr renders the single
+// view of f with the scene's own TLAS and lights; otherwise f is unused and each path
+// takes its frame constants, TLAS root, lights and AOV targets from its item.
+void launch_raygen(const FrameDev* f, const BatchDev& b, const WaveDev& w, uint64_t chunk_start, uint32_t chunk_n,
+                   cudaStream_t st);
+void launch_extend(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                   uint32_t depth, uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st);
+void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                  uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st);
+void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
+                   cudaStream_t st);
 // Persistent traversal with dynamic ray fetch (closest hit, or shadow rays when `shadow`).
 // Needs w.counters[3] (closest) / w.counters[4] (shadow) zeroed before the launch.
-void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint32_t depth,
-                      uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode, cudaStream_t st);
+void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                      uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
+                      cudaStream_t st);
 uint32_t trace_dyn_blocks_per_sm();
-void launch_gather(const SceneDev& s, const FrameDev* f, const WaveDev& w, int cur, uint64_t chunk_start,
+void launch_gather(const SceneDev& s, const BatchDev& b, const WaveDev& w, int cur, uint64_t chunk_start,
                    uint32_t grid, cudaStream_t st);
 void launch_resolve(const FrameDev* f, const float4* radiance, uint32_t npix, uint32_t spp, float4* accum,
                     dbl4* sum64, cudaStream_t st);
