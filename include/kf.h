@@ -274,6 +274,28 @@ typedef struct kf_batch_item {
 } kf_batch_item;
 KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint32_t count);
 
+/* Autotuner of batched rendering (no counterpart in kuafu, whose launch shapes are the
+ * ray-tracing pipeline's): measures the batch with one knob changed at a time —
+ * traversal kernel, paths in flight, launch grids, BLAS leaf size — each over `reps`
+ * timed batches after a warm-up, and leaves the renderer configured with the fastest
+ * (kf_renderer_get_config shows it). Results stay identical: every knob only changes
+ * how the same per-path arithmetic is scheduled, or the BVH that finds the same hits. */
+typedef struct kf_autotune_result {
+    uint32_t traversal;
+    uint32_t blas_leaf_size;
+    uint64_t max_paths_in_flight;
+    uint32_t grid_extend;      /* blocks of the thread-per-ray traversal kernels */
+    uint32_t grid_shade;       /* blocks of the shading / gather kernels */
+    uint32_t candidates;       /* configurations measured */
+    float best_ms;             /* median batch time of the chosen configuration */
+    float start_ms;            /* ... of the configuration the renderer had before */
+    uint32_t start_traversal;
+    uint32_t start_blas_leaf_size;
+    uint64_t start_max_paths_in_flight;
+} kf_autotune_result;
+KF_API int kf_renderer_autotune(kf_renderer r, const kf_batch_item* items, uint32_t count, uint32_t reps,
+                                kf_autotune_result* out);
+
 /* ---- tensor-core building blocks of the learned denoiser (device pointers; no
  * counterpart in kuafu, whose OptiX denoiser is closed code, denoiser.cpp:257-316) ---- */
 /* y[n,y,x,y_coff+co] = act(bias[co] + sum x[n,y+dy,x+dx,ci] * w[tap][co][ci]), NHWC BF16,

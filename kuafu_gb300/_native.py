@@ -130,6 +130,13 @@ class kf_batch_item(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", C.c_void_p), ("spp", C.c_uint32), ("pad", C.c_uint32)]
 
 
+class kf_autotune_result(C.Structure):
+    _fields_ = [("traversal", C.c_uint32), ("blas_leaf_size", C.c_uint32), ("max_paths_in_flight", C.c_uint64),
+                ("grid_extend", C.c_uint32), ("grid_shade", C.c_uint32), ("candidates", C.c_uint32),
+                ("best_ms", C.c_float), ("start_ms", C.c_float), ("start_traversal", C.c_uint32),
+                ("start_blas_leaf_size", C.c_uint32), ("start_max_paths_in_flight", C.c_uint64)]
+
+
 VP = C.c_void_p
 I = C.c_int
 U32 = C.c_uint32
@@ -217,6 +224,7 @@ PROTOTYPES = {
     "kf_camera_get_size": (I, [VP, C.POINTER(I), C.POINTER(I)]),
     "kf_camera_get_ubo": (I, [VP, C.POINTER(kf_camera_ubo)]),
     "kf_renderer_run_batch": (I, [VP, C.POINTER(kf_batch_item), U32]),
+    "kf_renderer_autotune": (I, [VP, C.POINTER(kf_batch_item), U32, U32, C.POINTER(kf_autotune_result)]),
     "kf_relmse": (I, [VP, VP, VP, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
     "kf_relmse_noalloc": (I, [VP, VP, C.c_uint64, C.c_double, VP, C.POINTER(C.c_double)]),
     "kf_conv3x3_bf16": (I, [VP, I, I, I, I, VP, I, VP, I, I, VP, I, I, VP]),

@@ -497,13 +497,25 @@ class Kuafu:
     def countTraversal(self, enable: bool):
         N.check(_lib().kf_renderer_count_traversal(self._h, int(bool(enable))))
 
-    def runBatch(self, items):
+    @staticmethod
+    def _batch(items):
         arr = (N.kf_batch_item * len(items))()
         for i, (scene, cam, spp) in enumerate(items):
             arr[i].scene = scene._h.value
             arr[i].camera = cam._h.value
             arr[i].spp = int(spp)
-        N.check(_lib().kf_renderer_run_batch(self._h, arr, len(items)))
+        return arr
+
+    def runBatch(self, items):
+        """One frame of every (scene, camera, spp) in one wavefront (kf_renderer_run_batch)."""
+        N.check(_lib().kf_renderer_run_batch(self._h, self._batch(items), len(items)))
+
+    def autotune(self, items, reps: int = 2) -> N.kf_autotune_result:
+        """Measures launch configurations on this batch and keeps the fastest."""
+        res = N.kf_autotune_result()
+        N.check(_lib().kf_renderer_autotune(self._h, self._batch(items), len(items), int(reps), C.byref(res)))
+        N.check(_lib().kf_renderer_get_config(self._h, C.byref(self.config._c)))
+        return res
 
     def setDenoiser(self, denoiser: "Denoiser | None"):
         """Denoiser that run() applies when the config's use_denoiser is set."""

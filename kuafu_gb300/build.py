@@ -38,6 +38,7 @@ SOURCES = [
     ("kf_wavefront.cu", ["-fmad=false"]),
     ("kf_conv.cu", []),
     ("kf_denoise.cu", []),
+    ("kf_autotune.cu", []),
     ("kf_mesh.cpp", []),
 ]
 

@@ -340,24 +340,41 @@ KF_API int kf_renderer_run(kf_renderer r) {
     });
 }
 
+// Validated copy of a batch: scenes of this renderer, cameras of their scene, each once.
+static std::vector<kf_batch_item> checked_batch(kf_renderer r, const kf_batch_item* items, uint32_t count) {
+    REQ(r && (items || count == 0), "null argument");
+    require_device(r);
+    KF_CUDA_CHECK(cudaSetDevice(r->device));
+    std::vector<kf_batch_item> v(items, items + count);
+    for (uint32_t i = 0; i < count; ++i) {
+        kf_scene_s* s = check_scene(v[i].scene);
+        kf_camera_s* c = check_camera(v[i].camera);
+        REQ(c->scene == s, "batch camera does not belong to its scene");
+        REQ(std::find_if(r->scenes.begin(), r->scenes.end(), [&](auto& p) { return p.get() == s; }) !=
+                r->scenes.end(),
+            "batch scene does not belong to this renderer");
+        for (uint32_t j = 0; j < i; ++j) REQ(v[j].camera != c, "a camera appears twice in one batch");
+        camera_update_view(c);
+        if (!v[i].spp) v[i].spp = r->cfg.spp;
+    }
+    return v;
+}
+
 KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint32_t count) {
     return guarded([&] {
-        REQ(r && (items || count == 0), "null argument");
-        require_device(r);
-        KF_CUDA_CHECK(cudaSetDevice(r->device));
-        std::vector<kf_batch_item> v(items, items + count);
-        for (uint32_t i = 0; i < count; ++i) {
-            kf_scene_s* s = check_scene(v[i].scene);
-            kf_camera_s* c = check_camera(v[i].camera);
-            REQ(c->scene == s, "batch camera does not belong to its scene");
-            REQ(std::find_if(r->scenes.begin(), r->scenes.end(), [&](auto& p) { return p.get() == s; }) !=
-                    r->scenes.end(),
-                "batch scene does not belong to this renderer");
-            for (uint32_t j = 0; j < i; ++j) REQ(v[j].camera != c, "a camera appears twice in one batch");
-            camera_update_view(c);
-            if (!v[i].spp) v[i].spp = r->cfg.spp;
-        }
+        std::vector<kf_batch_item> v = checked_batch(r, items, count);
         if (count) render_batch(r, v.data(), count);
+    });
+}
+
+KF_API int kf_renderer_autotune(kf_renderer r, const kf_batch_item* items, uint32_t count, uint32_t reps,
+                                kf_autotune_result* out) {
+    return guarded([&] {
+        std::vector<kf_batch_item> v = checked_batch(r, items, count);
+        REQ(count > 0, "empty batch");
+        REQ(!r->cfg.profile && !r->count_traversal, "autotune measures the production path: profile and "
+                                                    "traversal counting must be off");
+        autotune_batch(r, v.data(), count, reps, out);
     });
 }
 

@@ -1,0 +1,132 @@
+// kf_autotune.cu — picks the launch configuration of batched rendering by measurement:
+// traversal kernel (thread per ray / persistent dynamic fetch), wavefront chunk size
+// (paths in flight), launch grids of the per-ray kernels and the BLAS leaf size (the BVH
+// shape), one knob at a time (coordinate descent), each candidate timed with CUDA events
+// on the renderer's stream over `reps` batches after one warm-up batch (which also
+// captures the batch graph and, for a new leaf size, rebuilds every BLAS).
+#include <algorithm>
+#include <vector>
+
+#include "kf_host.h"
+
+namespace kf {
+namespace {
+
+struct Knobs {
+    uint32_t traversal;
+    uint64_t chunk;
+    uint32_t grid_extend, grid_shade;
+    uint32_t leaf;
+};
+
+void apply(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes, const Knobs& k) {
+    r->cfg.traversal = k.traversal;
+    r->cfg.max_paths_in_flight = k.chunk;
+    r->grid_extend = k.grid_extend;
+    r->grid_shade = k.grid_shade;
+    if (r->cfg.blas_leaf_size != k.leaf) {
+        r->cfg.blas_leaf_size = k.leaf;
+        for (kf_scene_s* s : scenes) ++s->geom_stamp; // rebuild every BLAS with the new leaf size
+    }
+}
+
+float time_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count, uint32_t reps) {
+    render_batch(r, items, count); // warm-up: rebuilds, graph capture
+    KF_CUDA_CHECK(cudaStreamSynchronize(r->stream));
+    cudaEvent_t e0 = r->ev[6], e1 = r->ev[7];
+    std::vector<float> t;
+    for (uint32_t i = 0; i < reps; ++i) {
+        KF_CUDA_CHECK(cudaEventRecord(e0, r->stream));
+        render_batch(r, items, count);
+        KF_CUDA_CHECK(cudaEventRecord(e1, r->stream));
+        KF_CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        t.push_back(ms);
+    }
+    std::sort(t.begin(), t.end());
+    return t[t.size() / 2];
+}
+
+} // namespace
+
+void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count, uint32_t reps,
+                    kf_autotune_result* out) {
+    KF_REQUIRE(count > 0, KF_ERR_INVALID_ARGUMENT, "empty batch");
+    reps = std::max(1u, reps);
+    std::vector<kf_scene_s*> scenes;
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (std::find(scenes.begin(), scenes.end(), items[i].scene) == scenes.end()) scenes.push_back(items[i].scene);
+        total += (uint64_t)items[i].camera->width * items[i].camera->height * items[i].spp;
+    }
+    const uint32_t sms = (uint32_t)std::max(1, r->num_sms);
+    Knobs best{r->cfg.traversal, r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24),
+               r->grid_extend, r->grid_shade, std::max(1u, r->cfg.blas_leaf_size)};
+    const Knobs start = best;
+    apply(r, scenes, best);
+    float best_ms = time_batch(r, items, count, reps);
+    const float start_ms = best_ms;
+    uint32_t tried = 1;
+    auto consider = [&](Knobs k) {
+        apply(r, scenes, k);
+        const float ms = time_batch(r, items, count, reps);
+        ++tried;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = k;
+        }
+    };
+    // 1. traversal kernel
+    {
+        Knobs k = best;
+        k.traversal = best.traversal ? 0u : 1u;
+        consider(k);
+    }
+    // 2. paths in flight (larger chunks: fewer launches; smaller: less memory traffic per bounce)
+    for (uint64_t c : {1ull << 22, 1ull << 23, 1ull << 24, 1ull << 25}) {
+        if (c == best.chunk || (c >> 1) >= total) continue;
+        Knobs k = best;
+        k.chunk = c;
+        consider(k);
+    }
+    // 3. launch grids (blocks per SM) of the shading / gather kernels and the thread-per-ray traversal
+    for (uint32_t m : {4u, 8u, 16u}) {
+        if (m * sms == best.grid_shade) continue;
+        Knobs k = best;
+        k.grid_shade = m * sms;
+        consider(k);
+    }
+    if (best.traversal == 0)
+        for (uint32_t m : {8u, 16u, 32u}) {
+            if (m * sms == best.grid_extend) continue;
+            Knobs k = best;
+            k.grid_extend = m * sms;
+            consider(k);
+        }
+    // 4. BVH shape: triangles per BLAS leaf
+    for (uint32_t leaf : {2u, 4u, 8u}) {
+        if (leaf == best.leaf) continue;
+        Knobs k = best;
+        k.leaf = leaf;
+        consider(k);
+    }
+    apply(r, scenes, best);
+    render_batch(r, items, count); // leaves the pools and graph of the winner in place
+    KF_CUDA_CHECK(cudaStreamSynchronize(r->stream));
+    if (out) {
+        out->traversal = best.traversal;
+        out->blas_leaf_size = best.leaf;
+        out->max_paths_in_flight = best.chunk;
+        out->grid_extend = best.grid_extend;
+        out->grid_shade = best.grid_shade;
+        out->candidates = tried;
+        out->best_ms = best_ms;
+        out->start_ms = start_ms;
+        out->start_traversal = start.traversal;
+        out->start_blas_leaf_size = start.leaf;
+        out->start_max_paths_in_flight = start.chunk;
+    }
+}
+
+} // namespace kf

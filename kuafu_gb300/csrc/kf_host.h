@@ -217,6 +217,9 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
 void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes);
 // One frame of every (scene, camera, spp) item in one wavefront (kf_renderer_run_batch).
 void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count);
+// kf_renderer_autotune (kf_autotune.cu)
+void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count, uint32_t reps,
+                    kf_autotune_result* out);
 
 // global tables
 std::vector<kf_material_gpu> flatten_materials();

@@ -200,6 +200,57 @@ def icospheres(renderer: api.Kuafu, width=1920, height=1080, count=256, level=4,
     return cam
 
 
+def batch_views(renderer: api.Kuafu, n_scenes=64, cams_per_scene=2, seed=0, min_side=128, max_side=1024,
+                spp_range=(1, 32), inst_range=(2, 400), level=4, variants=8):
+    """The batched workload: n_scenes Cornell rooms (seeded variations), each holding N
+    level-`level` icospheres (N log-uniform in inst_range; `variants` material variants,
+    one geometry each, shared by the instances), seen by cams_per_scene cameras of square
+    resolution log-uniform in [min_side, max_side] (multiples of 16) with spp uniform in
+    spp_range. Returns [(scene, camera, spp)]."""
+    rng = SplitMix64(seed ^ 0x5EED)
+    items = []
+    for k in range(n_scenes):
+        s = renderer.getScene() if k == 0 else renderer.createScene()
+        side = lambda: max(16, int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side))) / 16)) * 16)
+        w0 = side()
+        cam0 = cornell(renderer, w0, w0, scene=s, variation=seed * 1000 + k)
+        geoms = []
+        for v in range(variants):
+            mat = api.NiceMaterial(diffuseColor=(rng.uniform(), rng.uniform(), rng.uniform()),
+                                   roughness=rng.uniform(0.05, 1.0), metallic=1.0 if rng.uniform() < 0.3 else 0.0,
+                                   transmission=1.0 if rng.uniform() < 0.2 else 0.0, ior=1.45)
+            g = api.createIcosphere(level, mat)
+            s.submitGeometry(g)
+            geoms.append(g)
+        n = int(round(math.exp(rng.uniform(math.log(inst_range[0]), math.log(inst_range[1])))))
+        for i in range(n):
+            g = geoms[int(rng.uniform() * variants) % variants]
+            pos = (rng.uniform(-0.85, 0.85), rng.uniform(-0.85, 0.85), rng.uniform(-0.85, 0.85))
+            sc = math.exp(rng.uniform(math.log(0.02), math.log(0.12)))
+            s.submitGeometryInstance(api.instance(g, translate(*pos) @ quat_matrix(rng.uniform(), rng.uniform(),
+                                                                                   rng.uniform()) @
+                                                  scale(sc, sc, sc)))
+        cams = [cam0]
+        for c in range(1, cams_per_scene):
+            wc = side()
+            cam = s.createCamera(wc, wc)
+            cam.setPosition((-3.0 + rng.uniform(-0.3, 0.3), rng.uniform(-0.6, 0.6), rng.uniform(-0.4, 0.4)))
+            cam.setFront((1.0, rng.uniform(-0.15, 0.15), rng.uniform(-0.1, 0.1)))
+            cam.setUp((0.0, 0.0, 1.0))
+            pinhole(cam, wc, wc, 45.0)
+            cams.append(cam)
+        for cam in cams:
+            spp = spp_range[0] + int(rng.uniform() * (spp_range[1] - spp_range[0] + 1))
+            items.append((s, cam, min(spp, spp_range[1])))
+    return items
+
+
+def batch_config(depth=5, seed=0) -> api.Config:
+    cfg = cornell_config(spp=1, depth=depth, seed=seed)
+    cfg.setGeometryInstanceLimit(512)
+    return cfg
+
+
 def icosphere_config(spp=8, depth=8, seed=0, count=256) -> api.Config:
     cfg = api.Config()
     cfg.setPerPixelSampleRate(spp)

@@ -74,6 +74,36 @@ def test_batch_view_equals_single_run():
     assert np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_autotune_changes_speed_not_results():
+    """kf_renderer_autotune tries traversal kernels, chunk sizes, grids and BLAS leaf sizes;
+    whatever it keeps, the next batch is still exactly the oracle's render. The frame word of
+    that batch is the number of batches the tuner ran: (1 + reps) per candidate + 1."""
+    depth = 3
+    cfg = scenes.batch_config(depth=depth)
+    cfg.setDebugOutputs(True)
+    with api.Kuafu(cfg) as r:
+        items = scenes.batch_views(r, n_scenes=2, cams_per_scene=2, seed=3, min_side=32, max_side=64,
+                                   spp_range=(1, 3), inst_range=(3, 12), level=2, variants=2)
+        reps = 1
+        res = r.autotune(items, reps=reps)
+        assert res.candidates >= 8 and res.best_ms > 0 and res.best_ms <= res.start_ms
+        assert r.config._c.traversal == res.traversal and r.config._c.blas_leaf_size == res.blas_leaf_size
+        frame = res.candidates * (1 + reps) + 1
+        r.runBatch(items)
+        cams_seen = {}
+        for s, cam, spp in items:
+            idx = cams_seen.setdefault(id(s), 0) + 1
+            cams_seen[id(s)] = idx
+            paths = r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp)
+            w, h = cam._size()
+            ref = O.render(s.export(), cam.ubo(), w, h, O.push_constants(spp, depth), seed=0, frame=frame,
+                           camera_index=idx, use_bvh=True, want_hits=False)
+            g = paths[..., :3].astype(np.float64)
+            c = ref["paths"].astype(np.float64)
+            within = ((np.abs(g - c) / np.maximum(np.abs(c), 1e-6)).max(axis=-1) <= 1e-4).mean()
+            assert within >= 0.999, within
+
+
 def test_batch_replay_and_scene_change():
     """The captured batch graph replays; editing one scene rebuilds the batch pools."""
     cfg = scenes.cornell_config(spp=1, depth=3)
