@@ -270,7 +270,7 @@ class Scene:
         self._h = C.c_void_p(handle)
         self._geoms = []
         self._instances = []
-        self._lights = {}
+        self._lights = {}  # light object -> handle (the object is kept alive with its handle)
 
     def submitGeometry(self, g: Geometry):
         N.check(_lib().kf_scene_submit_geometry(self._h, g._h))
@@ -349,19 +349,26 @@ class Scene:
         c = N.kf_point_light(_f3(l.position), _f3(l.color), float(l.radius), float(l.strength))
         h = C.c_void_p()
         N.check(_lib().kf_scene_add_point_light(self._h, C.byref(c), C.byref(h)))
-        self._lights[id(l)] = h
+        self._lights[id(l)] = (l, h)
 
     def addActiveLight(self, l: ActiveLight):
         c = N.kf_active_light(_f16(l.viewMat), _f3(l.color), float(l.fov), float(l.strength), float(l.softness),
                               int(l.texID))
         h = C.c_void_p()
         N.check(_lib().kf_scene_add_active_light(self._h, C.byref(c), C.byref(h)))
-        self._lights[id(l)] = h
+        self._lights[id(l)] = (l, h)
 
     def removePointLight(self, l):
-        N.check(_lib().kf_scene_remove_light(self._h, self._lights.pop(id(l))))
+        N.check(_lib().kf_scene_remove_light(self._h, self._lights.pop(id(l))[1]))
 
     removeActiveLight = removePointLight
+
+    def removeLights(self):
+        """Removes the directional light and every point / active light added through this object."""
+        self.removeDirectionalLight()
+        for _, h in list(self._lights.values()):
+            N.check(_lib().kf_scene_remove_light(self._h, h))
+        self._lights.clear()
 
     def createCamera(self, width, height) -> Camera:
         h = C.c_void_p()

@@ -245,6 +245,47 @@ def batch_views(renderer: api.Kuafu, n_scenes=64, cams_per_scene=2, seed=0, min_
     return items
 
 
+def dot_pattern(width, height, density=0.05, seed=0) -> np.ndarray:
+    """Seeded binary dot pattern (RGBA8, white dots on black) for a structured-light projector."""
+    rng = np.random.default_rng(seed)
+    img = np.zeros((height, width, 4), np.uint8)
+    img[..., 3] = 255
+    img[..., :3][rng.random((height, width)) < density] = 255
+    return img
+
+
+def active_light_rig(renderer: api.Kuafu, count=64, seed=0, pattern=(1280, 720), ir=(848, 480), rgb=(1280, 720),
+                     density=0.05, baseline=0.055, level=4):
+    """Active light sensing: the icosphere scene trimmed to `count` instances, seen by an RGB
+    camera (the scene's own lights) and by two IR cameras `baseline` apart (scene units are
+    metres) that see only a structured-light projector: an active light whose texture is a
+    seeded binary dot pattern (kuafu's ActiveLight with texPath, rchit:262-316; the pattern
+    is stretched to the square frustum kuafu builds, scene.cpp:277-278). The IR response is
+    one channel of the IR views' radiance. Returns {"rgb": (scene, cam), "ir": [(scene, left),
+    (scene, right)], "pattern": texture id}."""
+    rgb_scene = renderer.getScene()
+    cam_rgb = icospheres(renderer, rgb[0], rgb[1], count=count, level=level, seed=seed, scene=rgb_scene)
+    ir_scene = renderer.createScene()
+    # the same objects, without the visible-light sources
+    ir_probe = icospheres(renderer, ir[0], ir[1], count=count, level=level, seed=seed, scene=ir_scene)
+    ir_scene.removeLights()
+    ir_scene.setClearColor((0.0, 0.0, 0.0, 1.0))
+    tex = api.createTexture(dot_pattern(pattern[0], pattern[1], density, seed), srgb=False)
+    eye = np.array([-30.0, 0.0, 0.0])
+    ir_scene.addActiveLight(api.ActiveLight(viewMat=look_at_view(eye, (0.0, 0.0, 0.0), (0.0, 0.0, 1.0)),
+                                            color=(1.0, 1.0, 1.0), fov=math.radians(60.0), strength=3000.0,
+                                            softness=0.0, texID=tex))
+    cams = []
+    for side in (-0.5, 0.5):
+        cam = ir_probe if side < 0 else ir_scene.createCamera(ir[0], ir[1])
+        cam.setPosition((-30.0, side * baseline, 0.0))
+        cam.setFront((1.0, 0.0, 0.0))
+        cam.setUp((0.0, 0.0, 1.0))
+        pinhole(cam, ir[0], ir[1], 50.0)
+        cams.append((ir_scene, cam))
+    return {"rgb": (rgb_scene, cam_rgb), "ir": cams, "pattern": tex}
+
+
 def batch_config(depth=5, seed=0) -> api.Config:
     cfg = cornell_config(spp=1, depth=depth, seed=seed)
     cfg.setGeometryInstanceLimit(512)
