@@ -299,6 +299,34 @@ def active_light_summary(device: int, steps: int = 3) -> dict:
         return {"error": f"{type(e).__name__}: {e}"}
 
 
+def run_denoiser_profile(reps: int) -> int:
+    """Profiling entry: `reps` 1920x1080 denoiser inferences (untrained weights: the time does
+    not depend on them) on a 1-spp Cornell frame; prints the CUDA-event time of each."""
+    import torch
+
+    from kuafu_gb300 import api, scenes
+
+    with api.Kuafu(scenes.cornell_config(spp=1, depth=5)) as r:
+        cam = scenes.cornell(r, 1920, 1080)
+        r.run()
+        r.synchronize()
+        d = api.Denoiser(r, seed=0)
+        stream = torch.cuda.ExternalStream(r.stream())
+        ms = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            d.apply(cam)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        from kuafu_gb300.denoise_eval import unet_flops
+        print(json.dumps({"denoiser_inference_ms": ms, "flops_per_frame": unet_flops(1080, 1920)}), flush=True)
+        d.close()
+    return 0
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -430,12 +458,15 @@ def run_ours(args):
         dom_ext = sp.extend_ms >= sp.shadow_ms
         k_bytes, k_ms = (ext_bytes, sp.extend_ms) if dom_ext else (sh_bytes, sp.shadow_ms)
         achieved = k_bytes / launches / (k_ms / launches / 1e3) / 1e9 if k_ms > 0 else None
+        if WORKLOAD.get("traversal", 1) == 1:
+            kname = "k_trace_dyn<closest-hit>" if dom_ext else "k_trace_dyn<shadow>"
+        else:
+            kname = "k_extend" if dom_ext else "k_shadow"
         traffic = None
         tf = ROOT / "profiles" / "traffic.json"
         if tf.exists():
             try:
-                traffic = json.loads(tf.read_text()).get("extend_dram_bytes_per_launch" if dom_ext else
-                                                         "shadow_dram_bytes_per_launch")
+                traffic = json.loads(tf.read_text()).get(kname + " dram_bytes_per_launch")
             except Exception:
                 traffic = None
         cpu = cpu_baseline_sample()
@@ -450,7 +481,7 @@ def run_ours(args):
                        "triangles": WORKLOAD["count"] * 20 * 4 ** WORKLOAD["level"],
                        "rays_per_frame": rays_per_frame, "l2": "flushed (512 MiB write) before every timed step",
                        "parallelism": f"replicas x{ws}"},
-            "roofline": {"bound": "hbm", "kernel": "k_extend" if dom_ext else "k_shadow",
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "peak_source": peak_kind,
@@ -495,6 +526,8 @@ def main():
     ap.add_argument("--no-denoise", action="store_true",
                     help="skip the time-to-relMSE experiment (denoiser training and 1080p evaluation)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 128-view workload")
+    ap.add_argument("--profile-denoiser", type=int, default=0, metavar="N",
+                    help="profiling: only N 1080p denoiser inferences")
     args = ap.parse_args()
     if args.traversal is not None:
         WORKLOAD["traversal"] = args.traversal
@@ -510,6 +543,8 @@ def main():
     build.build_libkf()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_denoiser:
+        return run_denoiser_profile(args.profile_denoiser)
     return run_ours(args)
 
 
