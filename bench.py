@@ -112,6 +112,10 @@ def build_scene(device: int, profile=False, debug=False):
     cfg.setDebugOutputs(debug)
     if "traversal" in WORKLOAD:
         cfg.setTraversal(WORKLOAD["traversal"])
+    if "bvh_builder" in WORKLOAD:
+        cfg.setBvhBuilder(WORKLOAD["bvh_builder"])
+    if "blas_leaf_size" in WORKLOAD:
+        cfg.setBlasLeafSize(WORKLOAD["blas_leaf_size"])
     r = api.Kuafu(cfg)
     cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
                             level=WORKLOAD["level"], seed=WORKLOAD["seed"])
@@ -526,11 +530,17 @@ def main():
     ap.add_argument("--no-denoise", action="store_true",
                     help="skip the time-to-relMSE experiment (denoiser training and 1080p evaluation)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 128-view workload")
+    ap.add_argument("--bvh-builder", type=int, default=None, help="0: GPU LBVH, 1: host binned SAH")
+    ap.add_argument("--leaf", type=int, default=None, help="BLAS leaf size")
     ap.add_argument("--profile-denoiser", type=int, default=0, metavar="N",
                     help="profiling: only N 1080p denoiser inferences")
     args = ap.parse_args()
     if args.traversal is not None:
         WORKLOAD["traversal"] = args.traversal
+    if args.bvh_builder is not None:
+        WORKLOAD["bvh_builder"] = args.bvh_builder
+    if args.leaf is not None:
+        WORKLOAD["blas_leaf_size"] = args.leaf
     if args.warmup < 3:
         args.warmup = 3
     if args.width:

@@ -73,7 +73,7 @@ typedef struct kf_config {
     uint32_t max_materials;        /* setMaterialLimit (default 256) */
     /* GB300 additions */
     uint32_t seed;                 /* Philox seed (key word 0 is seed ^ pixel_index) */
-    uint32_t blas_leaf_size;       /* max triangles per BVH leaf (default 4) */
+    uint32_t blas_leaf_size;       /* max triangles per BVH leaf (default 2) */
     uint32_t tlas_leaf_size;       /* max instances per TLAS leaf (default 1) */
     uint64_t max_paths_in_flight;  /* wavefront chunk size (default 1<<24) */
     uint32_t debug_outputs;        /* 1: keep per-path radiance and primary hits for download */
@@ -84,6 +84,8 @@ typedef struct kf_config {
                                       rendering calls then fail with KF_ERR_NO_DEVICE */
     uint32_t traversal;            /* 0: one thread per ray; 1: persistent warps with dynamic
                                       ray fetch (default). Both give identical results. */
+    uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order, fastest build); 1: host binned
+                                      SAH (default: fewer node visits per ray). Same hits. */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */

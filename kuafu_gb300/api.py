@@ -72,6 +72,7 @@ class Config:
     def setMaxPathsInFlight(self, n): self._c.max_paths_in_flight = int(n)
     def setHostOnly(self, flag): self._c.host_only = int(bool(flag))
     def setTraversal(self, mode): self._c.traversal = int(mode)
+    def setBvhBuilder(self, mode): self._c.bvh_builder = int(mode)
 
 
 @dataclass

@@ -193,7 +193,7 @@ KF_API void kf_config_init(kf_config* c) {
     c->max_textures = 128;
     c->max_materials = 256;
     c->seed = 0;
-    c->blas_leaf_size = 4;
+    c->blas_leaf_size = 2;
     c->tlas_leaf_size = 1;
     c->max_paths_in_flight = 1ull << 24;
     c->debug_outputs = 0;
@@ -202,6 +202,7 @@ KF_API void kf_config_init(kf_config* c) {
     c->device = 0;
     c->host_only = 0;
     c->traversal = 1;
+    c->bvh_builder = 1;
 }
 
 KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {

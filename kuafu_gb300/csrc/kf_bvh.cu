@@ -455,4 +455,231 @@ int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, De
     return total;
 }
 
+// ---------------------------------------------------------------------------
+// Host binned-SAH builder (Wald 2007, "On fast construction of SAH-based bounding
+// volume hierarchies": 32 bins per axis over the centroid bounds, cost = C_node +
+// sum_i SA_i / SA * N_i), then the 4-wide collapse of the binary tree.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct HBox {
+    float lo[3], hi[3];
+    void reset() {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = INFINITY;
+            hi[k] = -INFINITY;
+        }
+    }
+    void grow(const HBox& b) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], b.lo[k]);
+            hi[k] = std::max(hi[k], b.hi[k]);
+        }
+    }
+    float area() const {
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        if (!(dx >= 0.0f) || !(dy >= 0.0f) || !(dz >= 0.0f)) return 0.0f;
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct BNode {
+    HBox box;
+    int left, right; // -1: leaf
+    int first, count;
+};
+
+struct SahBuilder {
+    const float* lo;
+    const float* hi;
+    int max_leaf;
+    std::vector<uint32_t> idx;
+    std::vector<float> cen; // 3 per primitive
+    std::vector<BNode> nodes;
+
+    HBox prim_box(uint32_t p) const {
+        HBox b;
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] = lo[3 * p + k];
+            b.hi[k] = hi[3 * p + k];
+        }
+        return b;
+    }
+
+    int build(int begin, int end, int depth) {
+        const int node = (int)nodes.size();
+        nodes.push_back(BNode{});
+        HBox box, cb;
+        box.reset();
+        cb.reset();
+        for (int i = begin; i < end; ++i) {
+            box.grow(prim_box(idx[i]));
+            for (int k = 0; k < 3; ++k) {
+                cb.lo[k] = std::min(cb.lo[k], cen[3 * idx[i] + k]);
+                cb.hi[k] = std::max(cb.hi[k], cen[3 * idx[i] + k]);
+            }
+        }
+        const int n = end - begin;
+        if (n <= max_leaf) { // leaves never exceed max_leaf (traversal encodes <= 16 triangles)
+            nodes[node] = BNode{box, -1, -1, begin, n};
+            return node;
+        }
+        constexpr int kBins = 32;
+        float best_cost = INFINITY;
+        int best_axis = -1, best_bin = 0;
+        // from depth 48 on only median splits: bounds the recursion for any input
+        for (int axis = 0; axis < 3 && depth < 48; ++axis) {
+            const float ext = cb.hi[axis] - cb.lo[axis];
+            if (!(ext > 0.0f)) continue;
+            HBox bb[kBins];
+            int bc[kBins];
+            for (int b = 0; b < kBins; ++b) {
+                bb[b].reset();
+                bc[b] = 0;
+            }
+            const float scale = kBins / ext;
+            for (int i = begin; i < end; ++i) {
+                const uint32_t p = idx[i];
+                int b = (int)((cen[3 * p + axis] - cb.lo[axis]) * scale);
+                b = std::min(std::max(b, 0), kBins - 1);
+                bb[b].grow(prim_box(p));
+                ++bc[b];
+            }
+            float right_area[kBins];
+            int right_count[kBins];
+            HBox acc;
+            acc.reset();
+            int cnt = 0;
+            for (int b = kBins - 1; b > 0; --b) {
+                acc.grow(bb[b]);
+                cnt += bc[b];
+                right_area[b] = acc.area();
+                right_count[b] = cnt;
+            }
+            acc.reset();
+            cnt = 0;
+            for (int b = 0; b < kBins - 1; ++b) {
+                acc.grow(bb[b]);
+                cnt += bc[b];
+                if (cnt == 0 || right_count[b + 1] == 0) continue;
+                const float cost = acc.area() * (float)cnt + right_area[b + 1] * (float)right_count[b + 1];
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = axis;
+                    best_bin = b;
+                }
+            }
+        }
+        int mid;
+        if (best_axis < 0) { // all centroids coincide: split the range in half
+            mid = begin + n / 2;
+        } else {
+            const float ext = cb.hi[best_axis] - cb.lo[best_axis];
+            const float scale = kBins / ext;
+            auto it = std::partition(idx.begin() + begin, idx.begin() + end, [&](uint32_t p) {
+                int b = (int)((cen[3 * p + best_axis] - cb.lo[best_axis]) * scale);
+                b = std::min(std::max(b, 0), kBins - 1);
+                return b <= best_bin;
+            });
+            mid = (int)(it - idx.begin());
+            if (mid == begin || mid == end) mid = begin + n / 2;
+        }
+        const int l = build(begin, mid, depth + 1);
+        const int r = build(mid, end, depth + 1);
+        nodes[node] = BNode{box, l, r, begin, n};
+        return node;
+    }
+};
+
+} // namespace
+
+int build_wide_bvh_sah_host(const float* lo, const float* hi, int n, int max_leaf, std::vector<Node4>& out,
+                            std::vector<uint32_t>& order) {
+    out.clear();
+    order.clear();
+    if (n <= 0) return 0;
+    SahBuilder B;
+    B.lo = lo;
+    B.hi = hi;
+    B.max_leaf = std::max(1, max_leaf);
+    B.idx.resize(n);
+    B.cen.resize(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        B.idx[i] = (uint32_t)i;
+        for (int k = 0; k < 3; ++k) B.cen[3 * (size_t)i + k] = 0.5f * (lo[3 * (size_t)i + k] + hi[3 * (size_t)i + k]);
+    }
+    B.nodes.reserve(2 * (size_t)n);
+    const int root = B.build(0, n, 0);
+    order = B.idx;
+    // 4-wide collapse, breadth first so that the root is node 0
+    struct Item {
+        int bnode, slot;
+    };
+    std::vector<Item> queue{{root, 0}};
+    out.resize(1);
+    for (size_t qi = 0; qi < queue.size(); ++qi) {
+        const BNode& bn = B.nodes[queue[qi].bnode];
+        int ch[4];
+        int nc = 0;
+        if (bn.left < 0) {
+            ch[nc++] = queue[qi].bnode; // a structure that fits one leaf: one leaf child
+        } else {
+            ch[nc++] = bn.left;
+            ch[nc++] = bn.right;
+            while (nc < 4) {
+                int best = -1;
+                float best_sa = -1.0f;
+                for (int c = 0; c < nc; ++c) {
+                    const BNode& cn = B.nodes[ch[c]];
+                    if (cn.left < 0) continue;
+                    const float sa = cn.box.area();
+                    if (sa > best_sa) {
+                        best_sa = sa;
+                        best = c;
+                    }
+                }
+                if (best < 0) break;
+                const BNode& open = B.nodes[ch[best]];
+                ch[best] = open.left;
+                ch[nc++] = open.right;
+            }
+        }
+        float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
+        int cc[4], cn[4];
+        for (int c = 0; c < 4; ++c) {
+            if (c >= nc) {
+                lx[c] = ly[c] = lz[c] = INFINITY;
+                hx[c] = hy[c] = hz[c] = -INFINITY;
+                cc[c] = 0;
+                cn[c] = -1;
+                continue;
+            }
+            const BNode& b = B.nodes[ch[c]];
+            lx[c] = b.box.lo[0]; ly[c] = b.box.lo[1]; lz[c] = b.box.lo[2];
+            hx[c] = b.box.hi[0]; hy[c] = b.box.hi[1]; hz[c] = b.box.hi[2];
+            if (b.left < 0) {
+                cc[c] = b.first;
+                cn[c] = b.count;
+            } else {
+                const int slot = (int)out.size();
+                out.emplace_back();
+                queue.push_back(Item{ch[c], slot});
+                cc[c] = slot;
+                cn[c] = 0;
+            }
+        }
+        Node4 o;
+        o.lox = make_float4(lx[0], lx[1], lx[2], lx[3]);
+        o.hix = make_float4(hx[0], hx[1], hx[2], hx[3]);
+        o.loy = make_float4(ly[0], ly[1], ly[2], ly[3]);
+        o.hiy = make_float4(hy[0], hy[1], hy[2], hy[3]);
+        o.loz = make_float4(lz[0], lz[1], lz[2], lz[3]);
+        o.hiz = make_float4(hz[0], hz[1], hz[2], hz[3]);
+        o.child = make_int4(cc[0], cc[1], cc[2], cc[3]);
+        o.cnt = make_int4(cn[0], cn[1], cn[2], cn[3]);
+        out[queue[qi].slot] = o;
+    }
+    return (int)out.size();
+}
+
 } // namespace kf

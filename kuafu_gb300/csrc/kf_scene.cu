@@ -5,9 +5,11 @@
 // of RayTracer (src/core/rt/rt.cpp:142-495), with the driver's builder replaced
 // by the GPU LBVH of kf_bvh.cu.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <thread>
 
 #include "kf_bvh.h"
 #include "kf_host.h"
@@ -228,16 +230,54 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         DeviceBuffer<float4> lo, hi;
         DeviceBuffer<Node4> nodes;
         DeviceBuffer<uint32_t> order;
+        // host SAH builds of every BLAS, in parallel over geometries (bvh_builder = 1)
+        const bool sah = r->cfg.bvh_builder == 1;
+        std::vector<std::vector<Node4>> sah_nodes(sah ? ng : 0);
+        std::vector<std::vector<uint32_t>> sah_order(sah ? ng : 0);
+        if (sah) {
+            const int leaf = (int)std::max(1u, r->cfg.blas_leaf_size);
+            std::atomic<size_t> next{0};
+            auto work = [&]() {
+                std::vector<float> blo, bhi;
+                for (size_t gi; (gi = next.fetch_add(1)) < ng;) {
+                    const kf_geometry_s* g = s->geometries[gi];
+                    const size_t nt_g = g->indices.size() / 3;
+                    blo.resize(3 * nt_g);
+                    bhi.resize(3 * nt_g);
+                    for (size_t t = 0; t < nt_g; ++t)
+                        for (int k = 0; k < 3; ++k) {
+                            const float a = g->vertices[g->indices[3 * t + 0]].pos[k];
+                            const float b = g->vertices[g->indices[3 * t + 1]].pos[k];
+                            const float c = g->vertices[g->indices[3 * t + 2]].pos[k];
+                            blo[3 * t + k] = std::min(std::min(a, b), c);
+                            bhi[3 * t + k] = std::max(std::max(a, b), c);
+                        }
+                    build_wide_bvh_sah_host(blo.data(), bhi.data(), (int)nt_g, leaf, sah_nodes[gi], sah_order[gi]);
+                }
+            };
+            const unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+            std::vector<std::thread> pool;
+            for (unsigned i = 1; i < nthreads; ++i) pool.emplace_back(work);
+            work();
+            for (std::thread& t : pool) t.join();
+        }
         for (size_t gi = 0; gi < ng; ++gi) {
             const uint32_t ntri = geom[gi].z;
             if (ntri == 0) continue;
-            lo.resize(ntri, st);
-            hi.resize(ntri, st);
-            k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, geom[gi].x, geom[gi].y, ntri,
-                                                            lo.ptr, hi.ptr);
-            KF_CUDA_CHECK(cudaGetLastError());
-            const int nn = build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes,
-                                          order, st);
+            int nn;
+            if (sah) {
+                nodes.upload(sah_nodes[gi].data(), sah_nodes[gi].size(), st);
+                order.upload(sah_order[gi].data(), sah_order[gi].size(), st);
+                nn = (int)sah_nodes[gi].size();
+            } else {
+                lo.resize(ntri, st);
+                hi.resize(ntri, st);
+                k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, geom[gi].x, geom[gi].y,
+                                                                ntri, lo.ptr, hi.ptr);
+                KF_CUDA_CHECK(cudaGetLastError());
+                nn = build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes, order,
+                                    st);
+            }
             k_tri_gather<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, order.ptr, geom[gi].x,
                                                              geom[gi].y, ntri, G.tris.ptr + geom[gi].y);
             k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y,
@@ -348,8 +388,23 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             dlo.upload(blo.data(), nv, st);
             dhi.upload(bhi.data(), nv, st);
             dids.upload(ids.data(), nv, st);
-            const int nn = build_wide_bvh(dlo.ptr, dhi.ptr, (int)nv, (int)std::max(1u, r->cfg.tlas_leaf_size),
-                                          G.tlas_nodes, order, st);
+            int nn;
+            if (r->cfg.bvh_builder == 1) {
+                std::vector<float> flo(3 * (size_t)nv), fhi(3 * (size_t)nv);
+                for (uint32_t i = 0; i < nv; ++i) {
+                    flo[3 * i] = blo[i].x; flo[3 * i + 1] = blo[i].y; flo[3 * i + 2] = blo[i].z;
+                    fhi[3 * i] = bhi[i].x; fhi[3 * i + 1] = bhi[i].y; fhi[3 * i + 2] = bhi[i].z;
+                }
+                std::vector<Node4> hn;
+                std::vector<uint32_t> ho;
+                nn = build_wide_bvh_sah_host(flo.data(), fhi.data(), (int)nv,
+                                             (int)std::max(1u, r->cfg.tlas_leaf_size), hn, ho);
+                G.tlas_nodes.upload(hn.data(), hn.size(), st);
+                order.upload(ho.data(), ho.size(), st);
+            } else {
+                nn = build_wide_bvh(dlo.ptr, dhi.ptr, (int)nv, (int)std::max(1u, r->cfg.tlas_leaf_size),
+                                    G.tlas_nodes, order, st);
+            }
             G.tlas_inst.resize(nv, st);
             k_map_ids<<<(nv + 255) / 256, 256, 0, st>>>(order.ptr, dids.ptr, nv, G.tlas_inst.ptr);
             KF_CUDA_CHECK(cudaGetLastError());
