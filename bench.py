@@ -116,6 +116,8 @@ def build_scene(device: int, profile=False, debug=False):
         cfg.setBvhBuilder(WORKLOAD["bvh_builder"])
     if "blas_leaf_size" in WORKLOAD:
         cfg.setBlasLeafSize(WORKLOAD["blas_leaf_size"])
+    if "dyn_refill_below" in WORKLOAD or "dyn_steps" in WORKLOAD:
+        cfg.setDynamicFetch(WORKLOAD.get("dyn_refill_below", 24), WORKLOAD.get("dyn_steps", 16))
     r = api.Kuafu(cfg)
     cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
                             level=WORKLOAD["level"], seed=WORKLOAD["seed"])
@@ -238,7 +240,8 @@ def batched_summary(device: int, steps: int = 3) -> dict:
             "autotuned": tuned,
             "autotune": {"traversal": res.traversal, "blas_leaf_size": res.blas_leaf_size,
                          "max_paths_in_flight": res.max_paths_in_flight, "grid_extend": res.grid_extend,
-                         "grid_shade": res.grid_shade, "candidates": res.candidates,
+                         "grid_shade": res.grid_shade, "dyn_refill_below": res.dyn_refill_below,
+                         "dyn_steps": res.dyn_steps, "candidates": res.candidates,
                          "tune_set_ms_before": res.start_ms, "tune_set_ms_after": res.best_ms},
             "graph": "one CUDA graph per batch layout, replayed every batch",
             "seconds": time.perf_counter() - t0,
@@ -532,6 +535,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 128-view workload")
     ap.add_argument("--bvh-builder", type=int, default=None, help="0: GPU LBVH, 1: host binned SAH")
     ap.add_argument("--leaf", type=int, default=None, help="BLAS leaf size")
+    ap.add_argument("--dyn", type=int, nargs=2, default=None, metavar=("REFILL_BELOW", "STEPS"),
+                    help="persistent traversal scheduling")
     ap.add_argument("--profile-denoiser", type=int, default=0, metavar="N",
                     help="profiling: only N 1080p denoiser inferences")
     args = ap.parse_args()
@@ -541,6 +546,8 @@ def main():
         WORKLOAD["bvh_builder"] = args.bvh_builder
     if args.leaf is not None:
         WORKLOAD["blas_leaf_size"] = args.leaf
+    if args.dyn is not None:
+        WORKLOAD["dyn_refill_below"], WORKLOAD["dyn_steps"] = args.dyn
     if args.warmup < 3:
         args.warmup = 3
     if args.width:

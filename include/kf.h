@@ -73,7 +73,7 @@ typedef struct kf_config {
     uint32_t max_materials;        /* setMaterialLimit (default 256) */
     /* GB300 additions */
     uint32_t seed;                 /* Philox seed (key word 0 is seed ^ pixel_index) */
-    uint32_t blas_leaf_size;       /* max triangles per BVH leaf (default 2) */
+    uint32_t blas_leaf_size;       /* max triangles per BVH leaf (default 1) */
     uint32_t tlas_leaf_size;       /* max instances per TLAS leaf (default 1) */
     uint64_t max_paths_in_flight;  /* wavefront chunk size (default 1<<24) */
     uint32_t debug_outputs;        /* 1: keep per-path radiance and primary hits for download */
@@ -86,6 +86,10 @@ typedef struct kf_config {
                                       ray fetch (default). Both give identical results. */
     uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order, fastest build); 1: host binned
                                       SAH (default: fewer node visits per ray). Same hits. */
+    uint32_t dyn_refill_below;     /* persistent traversal: a warp fetches new rays when fewer
+                                      lanes than this are busy (1..32, default 24) */
+    uint32_t dyn_steps;            /* ... and runs this many traversal steps between fetches
+                                      (1..64, default 16) */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */
@@ -278,7 +282,8 @@ KF_API int kf_renderer_run_batch(kf_renderer r, const kf_batch_item* items, uint
 
 /* Autotuner of batched rendering (no counterpart in kuafu, whose launch shapes are the
  * ray-tracing pipeline's): measures the batch with one knob changed at a time —
- * traversal kernel, paths in flight, launch grids, BLAS leaf size — each over `reps`
+ * traversal kernel, paths in flight, launch grids, the persistent traversal's refill
+ * threshold and steps between refills, BLAS leaf size — each over `reps`
  * timed batches after a warm-up, and leaves the renderer configured with the fastest
  * (kf_renderer_get_config shows it). Results stay identical: every knob only changes
  * how the same per-path arithmetic is scheduled, or the BVH that finds the same hits. */
@@ -294,6 +299,8 @@ typedef struct kf_autotune_result {
     uint32_t start_traversal;
     uint32_t start_blas_leaf_size;
     uint64_t start_max_paths_in_flight;
+    uint32_t dyn_refill_below;   /* persistent traversal scheduling chosen */
+    uint32_t dyn_steps;
 } kf_autotune_result;
 KF_API int kf_renderer_autotune(kf_renderer r, const kf_batch_item* items, uint32_t count, uint32_t reps,
                                 kf_autotune_result* out);

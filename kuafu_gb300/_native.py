@@ -92,7 +92,8 @@ class kf_config(C.Structure):
                 ("max_materials", C.c_uint32), ("seed", C.c_uint32), ("blas_leaf_size", C.c_uint32),
                 ("tlas_leaf_size", C.c_uint32), ("max_paths_in_flight", C.c_uint64), ("debug_outputs", C.c_uint32),
                 ("profile", C.c_uint32), ("use_graph", C.c_uint32), ("device", C.c_uint32),
-                ("host_only", C.c_uint32), ("traversal", C.c_uint32), ("bvh_builder", C.c_uint32)]
+                ("host_only", C.c_uint32), ("traversal", C.c_uint32), ("bvh_builder", C.c_uint32),
+                ("dyn_refill_below", C.c_uint32), ("dyn_steps", C.c_uint32)]
 
 
 class kf_stats(C.Structure):
@@ -134,7 +135,8 @@ class kf_autotune_result(C.Structure):
     _fields_ = [("traversal", C.c_uint32), ("blas_leaf_size", C.c_uint32), ("max_paths_in_flight", C.c_uint64),
                 ("grid_extend", C.c_uint32), ("grid_shade", C.c_uint32), ("candidates", C.c_uint32),
                 ("best_ms", C.c_float), ("start_ms", C.c_float), ("start_traversal", C.c_uint32),
-                ("start_blas_leaf_size", C.c_uint32), ("start_max_paths_in_flight", C.c_uint64)]
+                ("start_blas_leaf_size", C.c_uint32), ("start_max_paths_in_flight", C.c_uint64),
+                ("dyn_refill_below", C.c_uint32), ("dyn_steps", C.c_uint32)]
 
 
 VP = C.c_void_p

@@ -193,7 +193,7 @@ KF_API void kf_config_init(kf_config* c) {
     c->max_textures = 128;
     c->max_materials = 256;
     c->seed = 0;
-    c->blas_leaf_size = 2;
+    c->blas_leaf_size = 1;
     c->tlas_leaf_size = 1;
     c->max_paths_in_flight = 1ull << 24;
     c->debug_outputs = 0;
@@ -203,6 +203,8 @@ KF_API void kf_config_init(kf_config* c) {
     c->host_only = 0;
     c->traversal = 1;
     c->bvh_builder = 1;
+    c->dyn_refill_below = 24;
+    c->dyn_steps = 16;
 }
 
 KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
@@ -230,7 +232,10 @@ KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
         // persistent grids: enough resident warps to hide traversal latency
         r->grid_extend = (uint32_t)r->num_sms * 16;
         r->grid_shade = (uint32_t)r->num_sms * 8;
-        if (!r->cfg.host_only) r->grid_dyn = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm();
+        if (!r->cfg.host_only) {
+            r->grid_dyn = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm(false);
+            r->grid_dyn_shadow = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm(true);
+        }
         // Kuafu::Kuafu (kuafu.cpp:27-63): a scene with a 1x1 camera; present mode adds
         // a camera of the initial size and makes it current.
         kf_scene_s* s = new_scene(r.get());

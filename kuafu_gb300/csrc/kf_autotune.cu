@@ -1,6 +1,7 @@
 // kf_autotune.cu — picks the launch configuration of batched rendering by measurement:
 // traversal kernel (thread per ray / persistent dynamic fetch), wavefront chunk size
-// (paths in flight), launch grids of the per-ray kernels and the BLAS leaf size (the BVH
+// (paths in flight), launch grids of the per-ray kernels, the persistent kernel's warp
+// scheduling (refill threshold, steps between refills) and the BLAS leaf size (the BVH
 // shape), one knob at a time (coordinate descent), each candidate timed with CUDA events
 // on the renderer's stream over `reps` batches after one warm-up batch (which also
 // captures the batch graph and, for a new leaf size, rebuilds every BLAS).
@@ -17,6 +18,7 @@ struct Knobs {
     uint64_t chunk;
     uint32_t grid_extend, grid_shade;
     uint32_t leaf;
+    uint32_t refill_below, steps; // persistent traversal's warp scheduling
 };
 
 void apply(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes, const Knobs& k) {
@@ -24,6 +26,8 @@ void apply(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes, const Knobs
     r->cfg.max_paths_in_flight = k.chunk;
     r->grid_extend = k.grid_extend;
     r->grid_shade = k.grid_shade;
+    r->cfg.dyn_refill_below = k.refill_below;
+    r->cfg.dyn_steps = k.steps;
     if (r->cfg.blas_leaf_size != k.leaf) {
         r->cfg.blas_leaf_size = k.leaf;
         for (kf_scene_s* s : scenes) ++s->geom_stamp; // rebuild every BLAS with the new leaf size
@@ -62,7 +66,8 @@ void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count
     }
     const uint32_t sms = (uint32_t)std::max(1, r->num_sms);
     Knobs best{r->cfg.traversal, r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24),
-               r->grid_extend, r->grid_shade, std::max(1u, r->cfg.blas_leaf_size)};
+               r->grid_extend, r->grid_shade, std::max(1u, r->cfg.blas_leaf_size), r->cfg.dyn_refill_below,
+               r->cfg.dyn_steps};
     const Knobs start = best;
     apply(r, scenes, best);
     float best_ms = time_batch(r, items, count, reps);
@@ -104,8 +109,23 @@ void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count
             k.grid_extend = m * sms;
             consider(k);
         }
+    // 3b. persistent traversal: refill threshold and steps between refills
+    if (best.traversal == 1) {
+        for (uint32_t rb : {16u, 24u, 28u, 32u}) {
+            if (rb == best.refill_below) continue;
+            Knobs k = best;
+            k.refill_below = rb;
+            consider(k);
+        }
+        for (uint32_t ns : {2u, 4u, 8u, 16u}) {
+            if (ns == best.steps) continue;
+            Knobs k = best;
+            k.steps = ns;
+            consider(k);
+        }
+    }
     // 4. BVH shape: triangles per BLAS leaf
-    for (uint32_t leaf : {2u, 4u, 8u}) {
+    for (uint32_t leaf : {1u, 2u, 4u, 8u}) {
         if (leaf == best.leaf) continue;
         Knobs k = best;
         k.leaf = leaf;
@@ -120,6 +140,8 @@ void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count
         out->max_paths_in_flight = best.chunk;
         out->grid_extend = best.grid_extend;
         out->grid_shade = best.grid_shade;
+        out->dyn_refill_below = best.refill_below;
+        out->dyn_steps = best.steps;
         out->candidates = tried;
         out->best_ms = best_ms;
         out->start_ms = start_ms;

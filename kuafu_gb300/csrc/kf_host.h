@@ -176,7 +176,8 @@ struct kf_renderer_s {
     kf::DeviceBuffer<double> scratch64;
     kf_stats stats{};
     bool count_traversal = false;
-    uint32_t grid_extend = 0, grid_shade = 0, grid_dyn = 0;
+    uint32_t grid_extend = 0, grid_shade = 0;
+    uint32_t grid_dyn = 0, grid_dyn_shadow = 0; // persistent traversal: one resident wave each
     // CUDA graph of one frame's launch sequence
     cudaGraphExec_t graph_exec = nullptr;
     std::string graph_key;

@@ -250,14 +250,16 @@ static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* 
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 3 * sizeof(uint32_t), st));
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[0], st));
             if (dyn)
-                launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal, st);
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal,
+                                 r->cfg.dyn_refill_below, r->cfg.dyn_steps, st);
             else
                 launch_extend(sv, fd, b, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[1], st));
             launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[2], st));
             if (dyn)
-                launch_trace_dyn(sv, fd, b, w, cur, depth, start, true, r->grid_dyn, r->count_traversal, st);
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, true, r->grid_dyn_shadow, r->count_traversal,
+                                 r->cfg.dyn_refill_below, r->cfg.dyn_steps, st);
             else
                 launch_shadow(sv, b, w, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[3], st));
@@ -315,6 +317,14 @@ static FrameDev make_frame(const kf_renderer_s* r, const kf_scene_s* s, const kf
     return f;
 }
 
+// Launch-shape parameters baked into a captured graph (grids, persistent-kernel scheduling).
+static std::string launch_shape_key(const kf_renderer_s* r) {
+    char b[96];
+    std::snprintf(b, sizeof(b), "%u,%u,%u,%u,%u,%u", r->grid_extend, r->grid_shade, r->grid_dyn,
+                  r->grid_dyn_shadow, r->cfg.dyn_refill_below, r->cfg.dyn_steps);
+    return b;
+}
+
 static uint32_t chunk_for(const kf_renderer_s* r, uint64_t npaths) {
     uint64_t cap = r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24);
     cap = std::min<uint64_t>(cap, (1ull << 26) - 1);
@@ -353,11 +363,11 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
         // The launch sequence depends only on buffer addresses and sizes; the
         // per-frame values live in frame_dev, so a captured graph replays as is.
         char key[512];
-        std::snprintf(key, sizeof(key), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u", (void*)s, (void*)c,
+        std::snprintf(key, sizeof(key), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u|%s", (void*)s, (void*)c,
                       (unsigned long long)s->gpu.generation, npix, spp, r->cfg.path_depth,
                       (unsigned long long)npaths, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)w.contrib,
                       (void*)c->accum.ptr, (void*)w.primary, sv.num_slots,
-                      r->cfg.russian_roulette | (r->cfg.traversal << 1));
+                      r->cfg.russian_roulette | (r->cfg.traversal << 1), launch_shape_key(r).c_str());
         if (!r->graph_exec || r->graph_key != key) {
             if (r->graph_exec) {
                 cudaGraphExecDestroy(r->graph_exec);
@@ -480,7 +490,7 @@ void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count) 
         std::snprintf(buf, sizeof(buf), "%llu|%u|%llu|%u|%p|%p|%p|%u|%u|", (unsigned long long)B.generation, count,
                       (unsigned long long)total, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)B.items.ptr,
                       r->cfg.path_depth, r->cfg.russian_roulette | (r->cfg.traversal << 1));
-        key = buf;
+        key = buf + launch_shape_key(r) + "|";
         for (uint32_t i = 0; i < count; ++i) {
             std::snprintf(buf, sizeof(buf), "%p,%u,%u;", (void*)items[i].camera->accum.ptr, hv[i].f.npix,
                           items[i].spp);

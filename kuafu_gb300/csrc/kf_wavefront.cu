@@ -980,17 +980,19 @@ __global__ void __launch_bounds__(128) k_shadow(SceneDev s, BatchDev b, WaveDev 
 
 // ---------------------------------------------------------------------------
 // Persistent traversal with dynamic ray fetch. Each warp keeps up to 32 rays in
-// flight; whenever fewer than kRefillBelow lanes are busy, the idle lanes take
+// flight; whenever fewer than refill_below lanes are busy, the idle lanes take
 // the next rays of the queue (one ballot, one atomic per warp), so a warp does
 // not idle behind its slowest ray. Results are identical to k_extend / k_shadow:
 // each ray runs the same Tracer steps, only the interleaving changes.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kRefillBelow = 24;
-constexpr int kStepsPerRefill = 8;
-
+// refill_below: a warp fetches rays when fewer lanes than this are busy; steps: traversal
+// steps between fetches (both tunable, kf_config.dyn_refill_below / dyn_steps).
+// Occupancy: 7 resident blocks per SM for closest-hit rays (72 registers, a few bytes of
+// spill) and 8 for shadow rays (64 registers) measured fastest on the 256-icosphere frame.
 template <bool SHADOW, bool COUNT, bool BATCH>
-__global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b,
-                                                   WaveDev w, int cur, uint32_t depth, uint64_t chunk_start) {
+__global__ void __launch_bounds__(128, SHADOW ? 8 : 7)
+    k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, int cur, uint32_t depth,
+                uint64_t chunk_start, uint32_t refill_below, int steps) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
     const uint32_t count = SHADOW ? w.counters[2] : w.counters[cur];
     uint32_t* fetch = w.counters + (SHADOW ? 4 : 3);
@@ -1010,7 +1012,7 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* _
     uint32_t idx = 0;
     for (;;) {
         uint32_t act = __ballot_sync(kFull, active);
-        if (!exhausted && (uint32_t)__popc(act) < kRefillBelow) {
+        if (!exhausted && (uint32_t)__popc(act) < refill_below) {
             const bool need = !active;
             const uint32_t m = __ballot_sync(kFull, need);
             uint32_t base = 0;
@@ -1044,7 +1046,7 @@ __global__ void __launch_bounds__(128) k_trace_dyn(SceneDev s, const FrameDev* _
         if (active) {
             bool done = false;
 #pragma unroll 1
-            for (int k = 0; k < kStepsPerRefill && !done; ++k) done = t.step(s, SHADOW ? nullptr : &ah);
+            for (int k = 0; k < steps && !done; ++k) done = t.step(s, SHADOW ? nullptr : &ah);
             if (done) {
                 if (SHADOW) {
                     if (t.h.inst == kMiss) {
@@ -1242,34 +1244,38 @@ void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint3
 template <bool BATCH>
 static void trace_dyn_dispatch(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                                uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
-                               cudaStream_t st) {
+                               uint32_t rb, int ns, cudaStream_t st) {
     if (shadow) {
         if (count_mode)
-            k_trace_dyn<true, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+            k_trace_dyn<true, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start, rb, ns);
         else
-            k_trace_dyn<true, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+            k_trace_dyn<true, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start, rb, ns);
     } else {
         if (count_mode)
-            k_trace_dyn<false, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+            k_trace_dyn<false, true, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start, rb, ns);
         else
-            k_trace_dyn<false, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+            k_trace_dyn<false, false, BATCH><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start, rb, ns);
     }
 }
 void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                       uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
-                      cudaStream_t st) {
+                      uint32_t refill_below, uint32_t steps, cudaStream_t st) {
+    const uint32_t rb = std::min(std::max(refill_below, 1u), 32u);
+    const int ns = (int)std::min(std::max(steps, 1u), 64u);
     if (b.items)
-        trace_dyn_dispatch<true>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, st);
+        trace_dyn_dispatch<true>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, rb, ns, st);
     else
-        trace_dyn_dispatch<false>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, st);
+        trace_dyn_dispatch<false>(s, f, b, w, cur, depth, chunk_start, shadow, grid, count_mode, rb, ns, st);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
-uint32_t trace_dyn_blocks_per_sm() {
-    int a = 0, c = 0;
-    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<false, false, false>, 128, 0));
-    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_trace_dyn<true, false, false>, 128, 0));
-    return (uint32_t)std::max(1, std::min(a, c));
+uint32_t trace_dyn_blocks_per_sm(bool shadow) {
+    int a = 0;
+    if (shadow)
+        KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<true, false, false>, 128, 0));
+    else
+        KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_trace_dyn<false, false, false>, 128, 0));
+    return (uint32_t)std::max(1, a);
 }
 
 void launch_gather(const SceneDev& s, const BatchDev& b, const WaveDev& w, int cur, uint64_t chunk_start,

@@ -115,10 +115,12 @@ void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint3
                    cudaStream_t st);
 // Persistent traversal with dynamic ray fetch (closest hit, or shadow rays when `shadow`).
 // Needs w.counters[3] (closest) / w.counters[4] (shadow) zeroed before the launch.
+// refill_below (1..32) and steps (1..64): the warp scheduling of the persistent kernel.
 void launch_trace_dyn(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                       uint32_t depth, uint64_t chunk_start, bool shadow, uint32_t grid, bool count_mode,
-                      cudaStream_t st);
-uint32_t trace_dyn_blocks_per_sm();
+                      uint32_t refill_below, uint32_t steps, cudaStream_t st);
+// resident blocks per SM of the persistent traversal kernel (closest-hit or shadow variant)
+uint32_t trace_dyn_blocks_per_sm(bool shadow);
 void launch_gather(const SceneDev& s, const BatchDev& b, const WaveDev& w, int cur, uint64_t chunk_start,
                    uint32_t grid, cudaStream_t st);
 void launch_resolve(const FrameDev* f, const float4* radiance, uint32_t npix, uint32_t spp, float4* accum,
