@@ -713,7 +713,8 @@ __device__ bool light_sample(const SceneDev& s, const LS& ls, uint32_t slot, uin
 // Shade: miss / emission / PrincipledBSDF (rchit:322-468), light samples, RR.
 // ---------------------------------------------------------------------------
 template <bool BATCH>
-__global__ void __launch_bounds__(128) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+// 4 resident blocks per SM (128 registers, no spill) measured fastest; unbounded it takes 148.
+__global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                                int cur, uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[cur];
     const int nxt = cur ^ 1;
