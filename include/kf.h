@@ -149,6 +149,7 @@ typedef struct kf_stats {
     uint32_t last_spp;
     uint32_t blas_nodes;
     uint32_t tlas_nodes;
+    uint64_t tlas_refits;     /* TLAS refits (transform-only updates) of the current scene */
 } kf_stats;
 KF_API int kf_renderer_get_stats(kf_renderer r, kf_stats* out);
 KF_API int kf_renderer_reset_stats(kf_renderer r);

@@ -103,7 +103,7 @@ class kf_stats(C.Structure):
                 ("shadow_inst_visits", C.c_uint64), ("extend_ms", C.c_double), ("shadow_ms", C.c_double),
                 ("shade_ms", C.c_double), ("frame_ms", C.c_double), ("bvh_build_ms", C.c_double),
                 ("frame_count", C.c_int32), ("last_spp", C.c_uint32), ("blas_nodes", C.c_uint32),
-                ("tlas_nodes", C.c_uint32)]
+                ("tlas_nodes", C.c_uint32), ("tlas_refits", C.c_uint64)]
 
 
 class kf_material(C.Structure):

@@ -710,7 +710,7 @@ KF_API int kf_instance_set_transform(kf_instance i, const float transform[16]) {
         float rows[12];
         affine_inverse_rows(transform, rows);
         std::memcpy(i->transform, transform, sizeof(i->transform));
-        if (i->scene) ++i->scene->inst_stamp;
+        if (i->scene) ++i->scene->xform_stamp; // TLAS refit before the next frame
     });
 }
 KF_API int kf_scene_remove_instance(kf_scene s, kf_instance i) {

@@ -89,10 +89,15 @@ struct SceneGpu {
     std::vector<uint32_t> tri_offset, vert_offset;   // per geometry
     uint64_t built_geom_stamp = 0;
     uint64_t built_inst_stamp = 0;
+    uint64_t built_xform_stamp = 0;
+    std::vector<kf::Node4> tlas_host_nodes; // TLAS topology kept for refits
+    std::vector<uint32_t> tlas_host_inst;
+    uint64_t tlas_refits = 0;
     uint64_t built_material_version = 0;
     uint64_t built_texture_version = 0;
     uint32_t blas_node_count = 0, tlas_node_count = 0;
-    uint64_t generation = 0; // bumped whenever a device buffer may have moved
+    uint64_t generation = 0;      // bumped whenever a device buffer may have moved
+    uint64_t content_version = 0; // bumped whenever any device content changed
     kf::SceneDev view{};
 };
 
@@ -112,7 +117,8 @@ struct kf_scene_s {
     std::vector<std::unique_ptr<kf_camera_s>> cameras;
     kf_camera_s* current_camera = nullptr;
     uint64_t geom_stamp = 1;  // bumped on geometry set changes
-    uint64_t inst_stamp = 1;  // bumped on instance set / transform changes
+    uint64_t inst_stamp = 1;  // bumped on instance set changes (TLAS rebuild)
+    uint64_t xform_stamp = 1; // bumped on instance transform changes (TLAS refit)
     SceneGpu gpu;
     // export cache (kf_scene_export)
     std::vector<kf_flat_geometry> x_geoms;

@@ -176,7 +176,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         KF_CUDA_CHECK(cudaEventCreate(&e1));
         KF_CUDA_CHECK(cudaEventRecord(e0, st));
     }
-    bool built_any = false;
+    bool built_any = false, refitted = false;
     if (G.built_geom_stamp != s->geom_stamp) {
         built_any = true;
         rebuilt_geom = true;
@@ -334,18 +334,22 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         G.built_env_version = s->env_version;
         ++G.generation;
     }
-    if (rebuilt_geom || G.built_inst_stamp != s->inst_stamp) {
-        built_any = true;
+    // Instance records (world->object rows, BLAS root, flags) and padded world boxes of the
+    // visible instances; wlo / whi indexed by instance, ids = the visible instances.
+    auto instance_records = [&](std::vector<InstanceRec>& recs, std::vector<float4>& wlo,
+                                std::vector<float4>& whi, std::vector<uint32_t>& ids) {
         const size_t ni = s->instances.size();
-        std::vector<InstanceRec> recs(ni);
-        std::vector<float4> blo, bhi;
-        std::vector<uint32_t> ids;
+        recs.assign(ni, InstanceRec{});
+        wlo.assign(ni, make_float4(0, 0, 0, 0));
+        whi.assign(ni, make_float4(0, 0, 0, 0));
+        ids.clear();
         for (size_t i = 0; i < ni; ++i) {
             const kf_instance_s* in = s->instances[i];
             size_t gi = 0;
             for (; gi < s->geometries.size(); ++gi)
                 if (s->geometries[gi] == in->geometry) break;
-            KF_REQUIRE(gi < s->geometries.size(), KF_ERR_STATE, "instance references a geometry not submitted to the scene");
+            KF_REQUIRE(gi < s->geometries.size(), KF_ERR_STATE,
+                       "instance references a geometry not submitted to the scene");
             float rows[12];
             affine_inverse_rows(in->transform, rows);
             InstanceRec& rc = recs[i];
@@ -375,9 +379,71 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             double mag = 0.0;
             for (int k = 0; k < 3; ++k) mag = std::max(mag, std::max(std::fabs(mn[k]), std::fabs(mx[k])));
             const double pad = mag * 0x1.0p-16 + 1e-6;
-            blo.push_back(make_float4((float)(mn[0] - pad), (float)(mn[1] - pad), (float)(mn[2] - pad), 0.0f));
-            bhi.push_back(make_float4((float)(mx[0] + pad), (float)(mx[1] + pad), (float)(mx[2] + pad), 0.0f));
+            wlo[i] = make_float4((float)(mn[0] - pad), (float)(mn[1] - pad), (float)(mn[2] - pad), 0.0f);
+            whi[i] = make_float4((float)(mx[0] + pad), (float)(mx[1] + pad), (float)(mx[2] + pad), 0.0f);
             ids.push_back((uint32_t)i);
+        }
+    };
+    const bool set_changed = rebuilt_geom || G.built_inst_stamp != s->inst_stamp;
+    if (!set_changed && G.built_xform_stamp != s->xform_stamp) {
+        // Transforms moved, the instance set did not (RayTracer::updateTlas every frame,
+        // context.cpp:334-341): new world->object rows and world boxes; the TLAS keeps its
+        // topology and its node boxes are refitted children-first (children are always
+        // numbered after their parent). Buffers keep their size: no graph recapture.
+        refitted = true;
+        std::vector<InstanceRec> recs;
+        std::vector<float4> wlo, whi;
+        std::vector<uint32_t> ids;
+        instance_records(recs, wlo, whi, ids);
+        if (!recs.empty()) G.inst.upload(recs.data(), recs.size(), st);
+        std::vector<Node4>& nodes = G.tlas_host_nodes;
+        for (size_t n = nodes.size(); n-- > 0;) {
+            Node4& nd = nodes[n];
+            float lx[4], ly[4], lz[4], hx[4], hy[4], hz[4];
+            const int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
+            const int cn[4] = {nd.cnt.x, nd.cnt.y, nd.cnt.z, nd.cnt.w};
+            for (int c = 0; c < 4; ++c) {
+                lx[c] = ly[c] = lz[c] = INFINITY;
+                hx[c] = hy[c] = hz[c] = -INFINITY;
+                if (cn[c] < 0) continue;
+                if (cn[c] == 0) {
+                    const Node4& k = nodes[ch[c]];
+                    lx[c] = std::min(std::min(k.lox.x, k.lox.y), std::min(k.lox.z, k.lox.w));
+                    ly[c] = std::min(std::min(k.loy.x, k.loy.y), std::min(k.loy.z, k.loy.w));
+                    lz[c] = std::min(std::min(k.loz.x, k.loz.y), std::min(k.loz.z, k.loz.w));
+                    hx[c] = std::max(std::max(k.hix.x, k.hix.y), std::max(k.hix.z, k.hix.w));
+                    hy[c] = std::max(std::max(k.hiy.x, k.hiy.y), std::max(k.hiy.z, k.hiy.w));
+                    hz[c] = std::max(std::max(k.hiz.x, k.hiz.y), std::max(k.hiz.z, k.hiz.w));
+                } else {
+                    for (int q = 0; q < cn[c]; ++q) {
+                        const uint32_t id = G.tlas_host_inst[ch[c] + q];
+                        lx[c] = std::min(lx[c], wlo[id].x); ly[c] = std::min(ly[c], wlo[id].y);
+                        lz[c] = std::min(lz[c], wlo[id].z); hx[c] = std::max(hx[c], whi[id].x);
+                        hy[c] = std::max(hy[c], whi[id].y); hz[c] = std::max(hz[c], whi[id].z);
+                    }
+                }
+            }
+            nd.lox = make_float4(lx[0], lx[1], lx[2], lx[3]);
+            nd.loy = make_float4(ly[0], ly[1], ly[2], ly[3]);
+            nd.loz = make_float4(lz[0], lz[1], lz[2], lz[3]);
+            nd.hix = make_float4(hx[0], hx[1], hx[2], hx[3]);
+            nd.hiy = make_float4(hy[0], hy[1], hy[2], hy[3]);
+            nd.hiz = make_float4(hz[0], hz[1], hz[2], hz[3]);
+        }
+        if (!nodes.empty()) G.tlas_nodes.upload(nodes.data(), nodes.size(), st);
+        G.built_xform_stamp = s->xform_stamp;
+        ++G.tlas_refits;
+    }
+    if (set_changed) {
+        built_any = true;
+        std::vector<InstanceRec> recs;
+        std::vector<float4> wlo, whi;
+        std::vector<uint32_t> ids;
+        instance_records(recs, wlo, whi, ids);
+        std::vector<float4> blo, bhi;
+        for (uint32_t id : ids) {
+            blo.push_back(wlo[id]);
+            bhi.push_back(whi[id]);
         }
         G.inst.upload(recs.data(), std::max<size_t>(recs.size(), 0), st);
         if (recs.empty()) G.inst.resize(1, st);
@@ -408,16 +474,27 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             G.tlas_inst.resize(nv, st);
             k_map_ids<<<(nv + 255) / 256, 256, 0, st>>>(order.ptr, dids.ptr, nv, G.tlas_inst.ptr);
             KF_CUDA_CHECK(cudaGetLastError());
-            KF_CUDA_CHECK(cudaStreamSynchronize(st));
             G.tlas_node_count = (uint32_t)nn;
+            // host copies of the topology for later refits
+            G.tlas_host_nodes.resize(nn);
+            G.tlas_host_inst.resize(nv);
+            KF_CUDA_CHECK(cudaMemcpyAsync(G.tlas_host_nodes.data(), G.tlas_nodes.ptr, sizeof(Node4) * nn,
+                                          cudaMemcpyDeviceToHost, st));
+            KF_CUDA_CHECK(cudaMemcpyAsync(G.tlas_host_inst.data(), G.tlas_inst.ptr, sizeof(uint32_t) * nv,
+                                          cudaMemcpyDeviceToHost, st));
+            KF_CUDA_CHECK(cudaStreamSynchronize(st));
         } else {
             G.tlas_node_count = 0;
             G.tlas_nodes.resize(1, st);
             G.tlas_inst.resize(1, st);
+            G.tlas_host_nodes.clear();
+            G.tlas_host_inst.clear();
         }
         G.built_inst_stamp = s->inst_stamp;
+        G.built_xform_stamp = s->xform_stamp;
     }
-    if (built_any || rebuilt_geom) ++G.generation;
+    if (built_any || rebuilt_geom) ++G.generation;            // buffers may have moved: recapture graphs
+    if (built_any || rebuilt_geom || refitted) ++G.content_version; // contents changed: recopy batch pools
     if (timing) {
         KF_CUDA_CHECK(cudaEventRecord(e1, st));
         KF_CUDA_CHECK(cudaEventSynchronize(e1));
@@ -480,6 +557,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
     v.num_slots = ns;
     r->stats.blas_nodes = G.blas_node_count;
     r->stats.tlas_nodes = G.tlas_node_count;
+    r->stats.tlas_refits = G.tlas_refits;
 }
 
 // Concatenates the pools of the batch's scenes: vertex, index, material-index and
@@ -492,7 +570,7 @@ void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes) {
     if (!r->batch) r->batch = std::make_unique<BatchState>();
     BatchState& B = *r->batch;
     std::vector<uint64_t> gens;
-    for (kf_scene_s* s : scenes) gens.push_back(s->gpu.generation);
+    for (kf_scene_s* s : scenes) gens.push_back(s->gpu.content_version);
     if (B.scenes == scenes && B.generations == gens) {
         // lights and slot tables are refreshed by scene_sync_gpu every call; pools are current
         return;
