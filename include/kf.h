@@ -200,6 +200,13 @@ KF_API int kf_geometry_release(kf_geometry g);
 /* Procedural meshes (geometry.cpp:297-537) plus the level-n icosphere. */
 enum { KF_MESH_YZ_PLANE = 0, KF_MESH_CUBE = 1, KF_MESH_SPHERE = 2, KF_MESH_CAPSULE = 3, KF_MESH_ICOSPHERE = 4 };
 KF_API int kf_geometry_create_builtin(int kind, float param0, float param1, const kf_material* m, kf_geometry* out);
+/* loadScene / loadObj (geometry.hpp:56-57, geometry.cpp:46-265) for Wavefront OBJ + MTL:
+ * one geometry per material used (faces merged per material), per-corner vertices, fan
+ * triangulation, flat normals where the file has none, V flipped, materials mapped as
+ * kuafu maps assimp's keys (roughness from Ns) and deduplicated in the global table.
+ * Call with out = NULL to get the count; then with capacity >= count. Texture maps are
+ * not decoded. */
+KF_API int kf_load_scene(const char* path, int dynamic, kf_geometry* out, uint32_t capacity, uint32_t* count);
 
 /* ---- kuafu::Scene (include/core/scene.hpp:40-295, src/core/scene.cpp) ---- */
 KF_API int kf_scene_submit_geometry(kf_scene s, kf_geometry g);             /* submitGeometry */

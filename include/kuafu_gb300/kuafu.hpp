@@ -242,6 +242,34 @@ inline std::shared_ptr<Geometry> createCapsule(float halfHeight = 1., float radi
     return detail::builtin(KF_MESH_CAPSULE, halfHeight, radius, dynamic, mat);
 }
 
+// loadScene / loadObj (geometry.hpp:56-57): Wavefront OBJ + MTL
+inline std::vector<std::shared_ptr<Geometry>> loadScene(std::string_view fname, bool dynamic) {
+    const std::string p(fname);
+    uint32_t n = 0;
+    detail::check(kf_load_scene(p.c_str(), dynamic ? 1 : 0, nullptr, 0, &n));
+    std::vector<kf_geometry> hs(n);
+    detail::check(kf_load_scene(p.c_str(), dynamic ? 1 : 0, hs.data(), n, &n));
+    std::vector<std::shared_ptr<Geometry>> out;
+    for (kf_geometry h : hs) {
+        auto g = std::make_shared<Geometry>();
+        g->adopt(h);
+        g->path = p;
+        g->dynamic = dynamic;
+        if (!g->matIndex.empty()) { // geometry.cpp:226: opaque iff the material's alpha is 1
+            kf_material m{};
+            detail::check(kf_material_get(g->matIndex.front(), &m));
+            g->isOpaque = m.alpha >= 1.0f;
+        }
+        out.push_back(std::move(g));
+    }
+    return out;
+}
+inline std::shared_ptr<Geometry> loadObj(std::string_view path, bool dynamic = false) {
+    auto scene = loadScene(path, dynamic);
+    if (scene.size() != 1) throw std::runtime_error("complex scene! use loadScene");
+    return scene.front();
+}
+
 // include/core/light.hpp:9-39
 struct DirectionalLight {
     vec3 direction = {0, 0, -1};

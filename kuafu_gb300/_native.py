@@ -185,6 +185,7 @@ PROTOTYPES = {
     "kf_geometry_get_data": (I, [VP, VP, VP, VP]),
     "kf_geometry_release": (I, [VP]),
     "kf_geometry_create_builtin": (I, [I, F, F, C.POINTER(kf_material), C.POINTER(VP)]),
+    "kf_load_scene": (I, [C.c_char_p, I, C.POINTER(VP), U32, C.POINTER(U32)]),
     "kf_scene_submit_geometry": (I, [VP, VP]),
     "kf_scene_clear_geometries": (I, [VP]),
     "kf_scene_remove_geometry": (I, [VP, VP]),

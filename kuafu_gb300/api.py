@@ -183,6 +183,24 @@ def createIcosphere(level=4, mat: NiceMaterial | None = None) -> Geometry:
     return _builtin(N.KF_MESH_ICOSPHERE, mat, level)
 
 
+def loadScene(path, dynamic=False) -> list[Geometry]:
+    """kuafu::loadScene (geometry.hpp:56): Wavefront OBJ + MTL, one geometry per material."""
+    p = os.fsencode(path)
+    n = C.c_uint32()
+    N.check(_lib().kf_load_scene(p, int(dynamic), None, 0, C.byref(n)))
+    arr = (C.c_void_p * max(n.value, 1))()
+    N.check(_lib().kf_load_scene(p, int(dynamic), arr, n.value, C.byref(n)))
+    return [Geometry(arr[i]) for i in range(n.value)]
+
+
+def loadObj(path, dynamic=False) -> Geometry:
+    """kuafu::loadObj (geometry.hpp:57): a file holding exactly one geometry."""
+    scene = loadScene(path, dynamic)
+    if len(scene) != 1:
+        raise N.KfError(1, "complex scene! use loadScene")
+    return scene[0]
+
+
 @dataclass
 class GeometryInstance:
     """kuafu::GeometryInstance (geometry.hpp:48-54)."""

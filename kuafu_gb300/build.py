@@ -40,6 +40,7 @@ SOURCES = [
     ("kf_denoise.cu", []),
     ("kf_autotune.cu", []),
     ("kf_mesh.cpp", []),
+    ("kf_obj.cpp", []),
 ]
 
 

@@ -11,6 +11,7 @@
 
 #include "kf_denoise.h"
 #include "kf_host.h"
+#include "kf_obj.h"
 
 namespace kf {
 std::mutex& global_mutex() {
@@ -620,6 +621,41 @@ KF_API int kf_geometry_get_data(kf_geometry g, kf_vertex* v, uint32_t* idx, uint
 }
 KF_API int kf_geometry_release(kf_geometry g) {
     return guarded([&] { geometry_release(g); });
+}
+KF_API int kf_load_scene(const char* path, int dynamic, kf_geometry* out, uint32_t capacity, uint32_t* count) {
+    return guarded([&] {
+        REQ(path && count, "null argument");
+        std::vector<ObjMesh> meshes;
+        load_obj(path, meshes);
+        *count = (uint32_t)meshes.size();
+        if (!out) return;
+        KF_REQUIRE(capacity >= meshes.size(), KF_ERR_OUT_OF_RANGE, "output array too small for the scene's geometries");
+        // materials: reuse an identical entry of the global table (geometry.cpp:154-173)
+        std::vector<uint32_t> mat_idx(meshes.size());
+        {
+            std::lock_guard<std::mutex> lk(global_mutex());
+            for (size_t k = 0; k < meshes.size(); ++k) {
+                const kf_material& m = meshes[k].material;
+                size_t j = 0;
+                for (; j < g_materials.size(); ++j)
+                    if (std::memcmp(&g_materials[j], &m, sizeof(m)) == 0) break;
+                if (j == g_materials.size()) {
+                    g_materials.push_back(m);
+                    ++g_material_version;
+                }
+                mat_idx[k] = (uint32_t)j;
+            }
+        }
+        for (size_t k = 0; k < meshes.size(); ++k) {
+            auto g = new kf_geometry_s();
+            g->vertices = std::move(meshes[k].vertices);
+            g->indices = std::move(meshes[k].indices);
+            g->mat_index.assign(g->indices.size() / 3, mat_idx[k]);
+            g->opaque = meshes[k].material.alpha >= 1.0f; // geometry.cpp:226
+            g->dynamic_ = dynamic != 0;
+            out[k] = g;
+        }
+    });
 }
 KF_API int kf_geometry_create_builtin(int kind, float p0, float p1, const kf_material* m, kf_geometry* out) {
     return guarded([&] {

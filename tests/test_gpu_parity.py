@@ -147,6 +147,29 @@ def test_sah_built_bvh_finds_the_same_hits(leaf):
         _check_paths(paths, ref["paths"])
 
 
+def test_loaded_obj_renders_like_the_oracle(tmp_path):
+    """A quad-faced OBJ box without normals (fan triangulation, flat normals, MTL material
+    with Ns -> roughness) loaded by kf_load_scene, inside the Cornell box."""
+    verts = [(x, y, z) for x in (-0.3, 0.3) for y in (-0.3, 0.3) for z in (-0.9, -0.3)]
+    quads = [(1, 2, 4, 3), (5, 7, 8, 6), (1, 5, 6, 2), (3, 4, 8, 7), (1, 3, 7, 5), (2, 6, 8, 4)]
+    obj = ["mtllib box.mtl"] + [f"v {x} {y} {z}" for x, y, z in verts] + ["usemtl gold"] + \
+          [f"f {a} {b} {c} {d}" for a, b, c, d in quads]
+    (tmp_path / "box.obj").write_text("\n".join(obj) + "\n")
+    (tmp_path / "box.mtl").write_text("newmtl gold\nKd 0.9 0.7 0.2\nNs 400\n")
+    spp, depth = 4, 4
+    cfg = scenes.cornell_config(spp=spp, depth=depth, debug=True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, 48, 48)
+        s = r.getScene()
+        (g,) = api.loadScene(tmp_path / "box.obj")
+        s.submitGeometry(g)
+        s.submitGeometryInstance(api.instance(g, scenes.rot_axis("z", 25)))
+        paths, hits, rgba, ref = _render_pair(r, cam, spp, depth)
+        assert np.array_equal(hits["instance"], ref["hits"]["instance"])
+        assert (hits["instance"] == 8).any()  # the loaded box is seen
+        _check_paths(paths, ref["paths"])
+
+
 def _smooth_env(n, seed):
     """Six n x n faces of smooth positive radiance (float32 RGBA)."""
     rng = np.random.default_rng(seed)
