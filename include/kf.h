@@ -125,7 +125,10 @@ enum {
     KF_AOV_SUM_F64 = 4,       /* double4 per pixel: FP64 sum of every frame's finalColor */
     KF_AOV_PATH_RADIANCE = 5, /* float4 per path [spp][h][w] of the last frame (debug_outputs) */
     KF_AOV_PRIMARY_HITS = 6,  /* kf_hit per path [spp][h][w] of the last frame (debug_outputs) */
-    KF_AOV_DENOISED_F32 = 7   /* float4 per pixel: output of the learned denoiser */
+    KF_AOV_DENOISED_F32 = 7,  /* float4 per pixel: output of the learned denoiser */
+    KF_AOV_SEGMENTATION = 8   /* uint32 x 4 per pixel: instance, geometry, material, primitive of
+                                 the first hit of sample 0 (0xFFFFFFFF x 3, 0 on a miss); the
+                                 segmentation SAPIEN asks of kuafu (README.md:66-67) */
 };
 KF_API int kf_renderer_download_aov(kf_renderer r, kf_camera cam, int kind, void* out, size_t bytes);
 

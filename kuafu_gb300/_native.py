@@ -251,6 +251,7 @@ PROTOTYPES = {
 
 KF_AOV_RADIANCE_F32, KF_AOV_ALBEDO_F32, KF_AOV_NORMAL_F32, KF_AOV_DEPTH_F32 = 0, 1, 2, 3
 KF_AOV_SUM_F64, KF_AOV_PATH_RADIANCE, KF_AOV_PRIMARY_HITS, KF_AOV_DENOISED_F32 = 4, 5, 6, 7
+KF_AOV_SEGMENTATION = 8
 KF_MESH_YZ_PLANE, KF_MESH_CUBE, KF_MESH_SPHERE, KF_MESH_CAPSULE, KF_MESH_ICOSPHERE = 0, 1, 2, 3, 4
 
 ERRORS = {1: "invalid argument", 2: "out of range", 3: "limit exceeded", 4: "CUDA error", 5: "not implemented",

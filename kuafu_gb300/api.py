@@ -500,6 +500,8 @@ class Kuafu:
             out = np.empty((h, w), np.float32)
         elif kind == N.KF_AOV_SUM_F64:
             out = np.empty((h, w, 4), np.float64)
+        elif kind == N.KF_AOV_SEGMENTATION:
+            out = np.empty((h, w, 4), np.uint32)  # instance, geometry, material, primitive
         elif kind == N.KF_AOV_PATH_RADIANCE:
             out = np.empty((spp or self.stats().last_spp, h, w, 4), np.float32)
         elif kind == N.KF_AOV_PRIMARY_HITS:

@@ -437,6 +437,7 @@ KF_API int kf_renderer_download_aov(kf_renderer r, kf_camera cam, int kind, void
                 src = r->wave.primary.ptr + c->last_path_start;
                 need = (size_t)c->last_spp * npix * sizeof(kf_hit);
                 break;
+            case KF_AOV_SEGMENTATION: src = c->seg.ptr; need = npix * 16; break;
             case KF_AOV_DENOISED_F32:
                 KF_REQUIRE(c->denoised.count == npix, KF_ERR_STATE, "no denoised frame for this camera");
                 src = c->denoised.ptr;

@@ -59,6 +59,7 @@ struct kf_camera_s {
     kf::DeviceBuffer<kf::dbl4> sum64;
     kf::DeviceBuffer<float> depth;
     kf::DeviceBuffer<uchar4> bgra;
+    kf::DeviceBuffer<uint4> seg;
     bool has_frame = false;
     int target_w = 0, target_h = 0;
     // where this camera's paths of its last frame sit in the renderer's per-path buffers

@@ -167,6 +167,7 @@ void ensure_targets(kf_renderer_s* r, kf_camera_s* c) {
         c->albedo.resize(npix, r->stream);
         c->normal.resize(npix, r->stream);
         c->depth.resize(npix, r->stream);
+        c->seg.resize(npix, r->stream);
         c->bgra.resize(npix, r->stream);
         c->target_w = c->width;
         c->target_h = c->height;
@@ -228,6 +229,7 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
     w.albedo = c->albedo.ptr;
     w.normal = c->normal.ptr;
     w.depth = c->depth.ptr;
+    w.seg = c->seg.ptr;
     w.stats = W.stats.ptr;
     w.chunk_cap = W.chunk_cap;
     return w;
@@ -431,9 +433,11 @@ void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count) 
     std::vector<ItemDev> hv(count);
     uint64_t total = 0;
     uint32_t max_slots = 1;
-    std::vector<uint32_t> inst_base(scenes.size(), 0);
-    for (size_t k = 1; k < scenes.size(); ++k)
+    std::vector<uint32_t> inst_base(scenes.size(), 0), geom_base(scenes.size(), 0);
+    for (size_t k = 1; k < scenes.size(); ++k) {
         inst_base[k] = inst_base[k - 1] + (uint32_t)scenes[k - 1]->instances.size();
+        geom_base[k] = geom_base[k - 1] + (uint32_t)scenes[k - 1]->geometries.size();
+    }
     for (uint32_t i = 0; i < count; ++i) {
         kf_scene_s* s = items[i].scene;
         kf_camera_s* c = items[i].camera;
@@ -458,6 +462,8 @@ void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count) 
         it.albedo = c->albedo.ptr;
         it.normal = c->normal.ptr;
         it.depth = c->depth.ptr;
+        it.seg = c->seg.ptr;
+        it.geom_base = geom_base[k];
         max_slots = std::max(max_slots, sv.num_slots);
     }
     const uint32_t chunk = chunk_for(r, total);

@@ -916,7 +916,21 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
                     }
                 }
             }
-            if (depth == 0 && sample == 0) aov_depth[pix] = inst == kMiss ? 0.0f : hv.x;
+            if (depth == 0 && sample == 0) {
+                aov_depth[pix] = inst == kMiss ? 0.0f : hv.x;
+                uint4* aov_seg = BATCH ? vw.it->seg : w.seg;
+                if (aov_seg) {
+                    uint4 sg = make_uint4(kMiss, kMiss, kMiss, 0u);
+                    if (inst != kMiss) {
+                        const uint32_t gidx = __ldg(&s.inst[inst].geometry);
+                        const uint32_t prim = w.hit_prim[i];
+                        const uint32_t midx = __ldg(s.matidx + __ldg(s.geom + gidx).y + prim);
+                        sg = BATCH ? make_uint4(inst - vw.it->inst_base, gidx - vw.it->geom_base, midx, prim)
+                                   : make_uint4(inst, gidx, midx, prim);
+                    }
+                    aov_seg[pix] = sg;
+                }
+            }
         }
         // light slots: one warp-uniform loop, one ballot per slot
         uint64_t req = 0;

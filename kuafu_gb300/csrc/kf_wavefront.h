@@ -66,9 +66,12 @@ struct ItemDev {
     const float4* env;
     uint32_t env_size;
     uint32_t inst_base;       // first instance of the item's scene in the batch's instance pool
+    uint32_t geom_base;       // first geometry of the item's scene in the batch's geometry pool
+    uint32_t pad3;
     float4* albedo;
     float4* normal;
     float* depth;
+    uint4* seg;
 };
 
 // Batch description handed to the kernels (items == nullptr: a single-view frame).
@@ -97,6 +100,7 @@ struct WaveDev {
     float4* albedo;       // per pixel AOVs
     float4* normal;
     float* depth;
+    uint4* seg;           // per pixel {instance, geometry, material, primitive} of sample 0's first hit
     unsigned long long* stats; // [0] primary, [1] extension, [2] shadow, [3] nodes, [4] tris, [5] inst
     uint16_t* path_item;       // batched launch: item of each path of the chunk
     uint32_t chunk_cap;

@@ -27,6 +27,9 @@ def _check(r, scene, cam, cam_index, spp, depth, clear, use_bvh, env=False):
     # the resolved frame: finalColor = colors / spp, stored (independent single frame)
     rgba = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
     assert np.allclose(rgba[..., :3], ref["pixel"], rtol=1e-6, atol=1e-7)
+    # segmentation ids are scene-local in a batch too
+    from test_gpu_parity import check_segmentation
+    check_segmentation(r, scene, cam, spp)
     return paths
 
 

@@ -70,6 +70,32 @@ def test_cornell_primary_hits_and_path_radiance():
         assert np.array_equal(nrm[..., :3], ref["normal"])
 
 
+def check_segmentation(r, scene, cam, spp):
+    """KF_AOV_SEGMENTATION = {instance, geometry, material, primitive} of sample 0's first hit."""
+    seg = r.downloadAov(cam, N.KF_AOV_SEGMENTATION)
+    hits0 = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)[0]
+    flat = scene.export()
+    assert np.array_equal(seg[..., 0], hits0["instance"])
+    miss = hits0["instance"] == 0xFFFFFFFF
+    assert (seg[..., 1][miss] == 0xFFFFFFFF).all() and (seg[..., 3][miss] == 0).all()
+    for y, x in zip(*np.nonzero(~miss)):
+        inst = int(seg[y, x, 0])
+        gi = flat.instances[inst].geometry_index
+        assert seg[y, x, 1] == gi
+        assert seg[y, x, 3] == hits0["prim"][y, x]
+        assert seg[y, x, 2] == flat.geometries[gi].mat_index[int(seg[y, x, 3])]
+    return seg
+
+
+def test_segmentation_aov():
+    cfg = scenes.cornell_config(spp=2, depth=2, debug=True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, 40, 32)
+        r.run()
+        seg = check_segmentation(r, r.getScene(), cam, 2)
+        assert len(np.unique(seg[..., 0])) >= 6  # walls, boxes, light, background
+
+
 def test_frame_accumulation_and_srgb_frame():
     """frameCount running mean (rgen:151-163) and the B8G8R8A8_SRGB frame (config.hpp:144)."""
     spp = 2
