@@ -113,13 +113,17 @@ template <bool SHADOW, bool COUNT> struct Tracer {
     // Returns true when the traversal is over (stack empty, or the first hit of a shadow ray).
     // Stack entries: kPopTag (back to the TLAS), kInstTag | instance, kLeafTag | (n-1) << 26 |
     // first triangle (a BLAS leaf of n triangles), or a node index.
+    // The rare, cheap entries do not take a step of their own: a return to the TLAS goes on
+    // to the next entry (a TLAS node or instance), and an instance entry goes on to the root
+    // node of its BLAS, so the lanes of a warp mostly run the node or the leaf code together.
     __device__ __forceinline__ bool step(const SceneDev& s, AnyHitCtx* ah) {
         if (sp <= 0) return true;
-        const uint32_t e = stack.get(--sp);
+        uint32_t e = stack.get(--sp);
         if (e == kPopTag) {
             in_blas = false;
             r = wr;
-            return sp <= 0;
+            if (sp <= 0) return true;
+            e = stack.get(--sp); // below a return entry: a TLAS node or an instance entry
         }
         if ((e & 0xC0000000u) == kLeafTag) {
             const uint32_t first = e & 0x03FFFFFFu, cnt_tri = ((e >> 26) & 0xFu) + 1u;
@@ -159,8 +163,7 @@ template <bool SHADOW, bool COUNT> struct Tracer {
             in_blas = true;
             if (sp + 2 > kStack) return sp <= 0;
             stack.put(sp++, kPopTag);
-            stack.put(sp++, meta.x);
-            return false;
+            e = meta.x; // the BLAS root, visited in this step
         }
         const Node4 n = load_node(in_blas ? s.blas_nodes : s.tlas_nodes, e);
         if (COUNT) cnt.nodes++;
@@ -190,10 +193,12 @@ template <bool SHADOW, bool COUNT> struct Tracer {
                 }
             }
         }
-        // sort descending by entry distance (fixed network, registers only), then push:
-        // the nearest child ends on top of the stack
+        // sort by entry distance (fixed network, registers only), then push. Closest-hit rays
+        // sort descending, so the nearest child ends on top of the stack; shadow rays (ended by
+        // any hit) sort ascending and take the farthest child first, which visits fewer nodes
+        // per ray than nearest-first on the 256-icosphere frame (23 against 26).
 #define KF_CSWAP(a, b)                                                                                     \
-    if (it[a] < it[b]) {                                                                                   \
+    if (SHADOW ? it[a] > it[b] : it[a] < it[b]) {                                                          \
         const float tf = it[a];                                                                            \
         it[a] = it[b];                                                                                     \
         it[b] = tf;                                                                                        \
