@@ -121,7 +121,10 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         uint32_t e = stack.get(--sp);
         if (e == kPopTag) {
             in_blas = false;
-            r = wr;
+            // back in the TLAS only boxes are tested: origin and reciprocal direction
+            // (copying the shear terms too would keep them live in registers)
+            r.ox = wr.ox; r.oy = wr.oy; r.oz = wr.oz;
+            r.ix = wr.ix; r.iy = wr.iy; r.iz = wr.iz;
             if (sp <= 0) return true;
             e = stack.get(--sp); // below a return entry: a TLAS node or an instance entry
         }
