@@ -134,7 +134,9 @@ KF_DEV float kpow5(float x) {
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and the per-path sub-streams.
 // ---------------------------------------------------------------------------
-KF_DEV uint4 philox(uint4 c, uint2 k) {
+// Not inlined: the shading kernel draws from a dozen call sites, and one shared copy of
+// the ten rounds keeps its code (and register count) smaller.
+static __device__ __noinline__ uint4 philox(uint4 c, uint2 k) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
         if (r) {

@@ -485,7 +485,9 @@ __device__ __forceinline__ v3 uniformSphereSampling(Stream& st, const PathKey& p
 // Environment lookup of PathTrace.rmiss:14-29: texture(environmentMap, vec3(-d.y, d.z, -d.x)).
 // Face selection by the major axis and face coordinates (sc, tc) of the Vulkan / GL cube
 // rules; bilinear within the face, clamp to edge. env: 6 faces of env_size^2 texels.
-__device__ v3 env_lookup(const float4* env, uint32_t env_size, v3 d) {
+// Texture and environment lookups are not inlined: k_shade is bound by instruction fetch
+// (its largest stall is "no instruction"), and one copy each keeps the kernel smaller.
+__device__ __noinline__ v3 env_lookup(const float4* env, uint32_t env_size, v3 d) {
     const float rx = -d.y, ry = d.z, rz = -d.x;
     const float ax = fabsf(rx), ay = fabsf(ry), az = fabsf(rz);
     uint32_t face;
@@ -523,7 +525,7 @@ __device__ v3 env_lookup(const float4* env, uint32_t env_size, v3 d) {
 }
 
 // Texture lookup: bilinear, repeat, optional sRGB decode (vkCore.hpp:585,619-637).
-__device__ v3 texture_rgb(const SceneDev& s, int id, float u, float v) {
+__device__ __noinline__ v3 texture_rgb(const SceneDev& s, int id, float u, float v) {
     if (id < 0 || (uint32_t)id >= s.num_textures) return splat(1.0f);
     const uint4 ti = __ldg(s.tex_info + id);
     const float x = u * (float)ti.y - 0.5f;
