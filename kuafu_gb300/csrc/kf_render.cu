@@ -183,7 +183,7 @@ void ensure_wave(kf_renderer_s* r, uint32_t chunk, uint32_t slots, uint64_t npat
     if (W.chunk_cap < chunk) {
         W.q_o0.resize(chunk, st); W.q_o1.resize(chunk, st);
         W.q_d0.resize(chunk, st); W.q_d1.resize(chunk, st);
-        W.hit.resize(chunk, st); W.hit_prim.resize(chunk, st);
+        W.hit.resize(chunk, st); W.hit_prim.resize(chunk, st); W.sel.resize(chunk, st);
         W.weight.resize(chunk, st); W.nee_w.resize(chunk, st);
         W.req.resize(chunk, st);
         W.chunk_cap = chunk;
@@ -217,6 +217,7 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
     w.counters = W.counters.ptr;
     w.hit = W.hit.ptr;
     w.hit_prim = W.hit_prim.ptr;
+    w.sel = W.sel.ptr;
     w.weight = W.weight.ptr;
     w.nee_w = W.nee_w.ptr;
     w.req = W.req.ptr;
@@ -248,8 +249,8 @@ static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* 
         for (uint32_t depth = 0; depth <= max_depth; ++depth) {
             const bool dyn = r->cfg.traversal == 1;
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + (cur ^ 1), 0, sizeof(uint32_t), st));
-            // [2] shadow queue count, [3] / [4] dynamic-fetch cursors
-            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 3 * sizeof(uint32_t), st));
+            // [2] shadow queue count, [3] / [4] dynamic-fetch cursors, [5] rays that hit
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 4 * sizeof(uint32_t), st));
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[0], st));
             if (dyn)
                 launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal,
@@ -257,6 +258,7 @@ static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* 
             else
                 launch_extend(sv, fd, b, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[1], st));
+            launch_miss(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[2], st));
             if (dyn)

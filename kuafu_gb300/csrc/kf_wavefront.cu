@@ -722,17 +722,59 @@ __device__ bool light_sample(const SceneDev& s, const LS& ls, uint32_t slot, uin
 // ---------------------------------------------------------------------------
 // Shade: miss / emission / PrincipledBSDF (rchit:322-468), light samples, RR.
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Rays that missed (PathTrace.rmiss:12-31): environment map, else clear colour, added with
+// the path weight; the path ends. The rays that hit are listed in w.sel for k_shade, so
+// that its warps shade hits only.
+// ---------------------------------------------------------------------------
+template <bool BATCH>
+__global__ void k_miss(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, int cur, uint32_t depth,
+                       uint64_t chunk_start) {
+    const uint32_t count = w.counters[cur];
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count;
+         base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + lane;
+        const bool miss = i < count && __float_as_uint(w.hit[i].w) == kMiss;
+        const uint32_t pos = warp_append(i < count && !miss, &w.counters[5]);
+        if (i < count && !miss) w.sel[pos] = i;
+        if (!miss) continue;
+        const float4 qo = w.q_o[cur][i], qd = w.q_d[cur][i];
+        const uint32_t p = __float_as_uint(qo.w);
+        const uint64_t g = chunk_start + p;
+        const View<BATCH> vw = view_of<BATCH>(fp, b, w, chunk_start, p);
+        const FrameDev& f = *vw.f;
+        const float4* env = BATCH ? vw.it->env : s.env;
+        const uint32_t env_size = BATCH ? vw.it->env_size : s.env_size;
+        const float4 w4 = w.weight[p];
+        const v3 wold = mk(w4.x, w4.y, w4.z);
+        const float4 col4 = w.radiance[g];
+        v3 color = mk(col4.x, col4.y, col4.z);
+        const v3 emission = (f.pc.use_env_map && env) ? env_lookup(env, env_size, mk(qd.x, qd.y, qd.z))
+                                                       : ld3(f.pc.clear_color) * f.pc.clear_color[3];
+        color = color + emission * wold;
+        w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
+        w.req[p] = 0;
+        if (depth == 0 && vw.g < f.npix) { // sample 0 of the first bounce
+            const uint32_t pix = (uint32_t)vw.g;
+            (BATCH ? vw.it->depth : w.depth)[pix] = 0.0f;
+            uint4* aov_seg = BATCH ? vw.it->seg : w.seg;
+            if (aov_seg) aov_seg[pix] = make_uint4(kMiss, kMiss, kMiss, 0u);
+        }
+    }
+}
+
 template <bool BATCH>
 // 4 resident blocks per SM (128 registers, no spill) measured fastest; unbounded it takes 148.
 __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                                int cur, uint32_t depth, uint64_t chunk_start) {
-    const uint32_t count = w.counters[cur];
+    const uint32_t count = w.counters[5]; // rays of this bounce that hit (k_miss takes the others)
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count; base += stride) {
-        const uint32_t i = base + lane;
-        const bool valid = i < count;
+        const bool valid = base + lane < count;
+        const uint32_t i = valid ? w.sel[base + lane] : 0u; // queue position of the ray
         uint32_t p = 0;
         uint64_t g = 0;
         PathKey pk;
@@ -753,25 +795,17 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
             const uint32_t sample = (uint32_t)(vw.g / f.npix);
             const uint32_t pix = (uint32_t)(vw.g % f.npix);
             pk = PathKey{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
-            const float4* env = BATCH ? vw.it->env : s.env;
-            const uint32_t env_size = BATCH ? vw.it->env_size : s.env_size;
             float4* aov_albedo = BATCH ? vw.it->albedo : w.albedo;
             float4* aov_normal = BATCH ? vw.it->normal : w.normal;
             float* aov_depth = BATCH ? vw.it->depth : w.depth;
             const float4 hv = w.hit[i];
-            const uint32_t inst = __float_as_uint(hv.w);
+            const uint32_t inst = __float_as_uint(hv.w); // never kMiss here
             const float4 w4 = w.weight[p];
             const v3 wold = mk(w4.x, w4.y, w4.z);
             float4 col4 = w.radiance[g];
             v3 color = mk(col4.x, col4.y, col4.z);
             const v3 rayD = mk(qd.x, qd.y, qd.z);
-            if (inst == kMiss) {
-                // PathTrace.rmiss:12-31: environment map, else clear colour
-                const v3 emission = (f.pc.use_env_map && env) ? env_lookup(env, env_size, rayD)
-                                                               : ld3(f.pc.clear_color) * f.pc.clear_color[3];
-                color = color + emission * wold;
-                w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
-            } else {
+            {
                 const uint32_t prim = w.hit_prim[i];
                 const InstanceRec* ip = s.inst + inst;
                 const float4 m0 = __ldg(&ip->w2o0), m1 = __ldg(&ip->w2o1), m2 = __ldg(&ip->w2o2);
@@ -927,18 +961,14 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
                 }
             }
             if (depth == 0 && sample == 0) {
-                aov_depth[pix] = inst == kMiss ? 0.0f : hv.x;
+                aov_depth[pix] = hv.x;
                 uint4* aov_seg = BATCH ? vw.it->seg : w.seg;
                 if (aov_seg) {
-                    uint4 sg = make_uint4(kMiss, kMiss, kMiss, 0u);
-                    if (inst != kMiss) {
-                        const uint32_t gidx = __ldg(&s.inst[inst].geometry);
-                        const uint32_t prim = w.hit_prim[i];
-                        const uint32_t midx = __ldg(s.matidx + __ldg(s.geom + gidx).y + prim);
-                        sg = BATCH ? make_uint4(inst - vw.it->inst_base, gidx - vw.it->geom_base, midx, prim)
-                                   : make_uint4(inst, gidx, midx, prim);
-                    }
-                    aov_seg[pix] = sg;
+                    const uint32_t gidx = __ldg(&s.inst[inst].geometry);
+                    const uint32_t prim = w.hit_prim[i];
+                    const uint32_t midx = __ldg(s.matidx + __ldg(s.geom + gidx).y + prim);
+                    aov_seg[pix] = BATCH ? make_uint4(inst - vw.it->inst_base, gidx - vw.it->geom_base, midx, prim)
+                                         : make_uint4(inst, gidx, midx, prim);
                 }
             }
         }
@@ -1248,6 +1278,14 @@ void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const
         k_shade<true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     else
         k_shade<false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                 uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
+    if (b.items)
+        k_miss<true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    else
+        k_miss<false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,

@@ -85,9 +85,11 @@ struct BatchDev {
 struct WaveDev {
     float4* q_o[2];       // ray queue: origin.xyz + path id bits
     float4* q_d[2];       // ray queue: direction.xyz
-    uint32_t* counters;   // [0],[1] ray queue counts, [2] shadow count
+    uint32_t* counters;   // [0],[1] ray queue counts, [2] shadow count, [3],[4] fetch cursors,
+                          // [5] rays of the bounce that hit
     float4* hit;          // t, u, v, instance bits
     uint32_t* hit_prim;
+    uint32_t* sel;        // queue positions of this bounce's rays that hit ([5] of them)
     float4* weight;       // throughput carried to the next bounce
     float4* nee_w;        // throughput that scales this bounce's NEE
     uint64_t* req;        // shadow slots requested this bounce (bit j = slot j)
@@ -113,8 +115,11 @@ void launch_raygen(const FrameDev* f, const BatchDev& b, const WaveDev& w, uint6
                    cudaStream_t st);
 void launch_extend(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                    uint32_t depth, uint64_t chunk_start, uint32_t grid, bool count_mode, cudaStream_t st);
+// k_miss ends the paths whose ray missed and lists the others in w.sel; k_shade shades those.
 void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                   uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st);
+void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
+                 uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st);
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
                    cudaStream_t st);
 // Persistent traversal with dynamic ray fetch (closest hit, or shadow rays when `shadow`).
