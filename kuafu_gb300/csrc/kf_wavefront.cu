@@ -728,39 +728,82 @@ __device__ bool light_sample(const SceneDev& s, const LS& ls, uint32_t slot, uin
 // that its warps shade hits only.
 // ---------------------------------------------------------------------------
 template <bool BATCH>
-__global__ void k_miss(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, int cur, uint32_t depth,
-                       uint64_t chunk_start) {
+__device__ __forceinline__ void miss_path(const SceneDev& s, const FrameDev* fp, const BatchDev& b, const WaveDev& w,
+                                          int cur, uint32_t depth, uint64_t chunk_start, uint32_t i) {
+    const float4 qo = w.q_o[cur][i], qd = w.q_d[cur][i];
+    const uint32_t p = __float_as_uint(qo.w);
+    const uint64_t g = chunk_start + p;
+    const View<BATCH> vw = view_of<BATCH>(fp, b, w, chunk_start, p);
+    const FrameDev& f = *vw.f;
+    const float4* env = BATCH ? vw.it->env : s.env;
+    const uint32_t env_size = BATCH ? vw.it->env_size : s.env_size;
+    const float4 w4 = w.weight[p];
+    const v3 wold = mk(w4.x, w4.y, w4.z);
+    const float4 col4 = w.radiance[g];
+    v3 color = mk(col4.x, col4.y, col4.z);
+    const v3 emission = (f.pc.use_env_map && env) ? env_lookup(env, env_size, mk(qd.x, qd.y, qd.z))
+                                                   : ld3(f.pc.clear_color) * f.pc.clear_color[3];
+    color = color + emission * wold;
+    w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
+    w.req[p] = 0;
+    if (depth == 0 && vw.g < f.npix) { // sample 0 of the first bounce
+        const uint32_t pix = (uint32_t)vw.g;
+        (BATCH ? vw.it->depth : w.depth)[pix] = 0.0f;
+        uint4* aov_seg = BATCH ? vw.it->seg : w.seg;
+        if (aov_seg) aov_seg[pix] = make_uint4(kMiss, kMiss, kMiss, 0u);
+    }
+}
+
+// One block of kMissThreads takes tiles of kMissThreads * kMissPer rays, kMissPer consecutive
+// rays per thread; the hits of a tile get their list positions from one atomic per tile (a
+// block scan), not one per warp, and stay in queue order (the order k_shade appends the next
+// bounce's rays in, which keeps neighbouring rays together).
+constexpr uint32_t kMissThreads = 128, kMissPer = 4;
+template <bool BATCH>
+__global__ void __launch_bounds__(kMissThreads) k_miss(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b,
+                                                       WaveDev w, int cur, uint32_t depth, uint64_t chunk_start) {
+    __shared__ uint32_t s_cnt[kMissThreads / 32];
+    __shared__ uint32_t s_base;
     const uint32_t count = w.counters[cur];
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count;
-         base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + lane;
-        const bool miss = i < count && __float_as_uint(w.hit[i].w) == kMiss;
-        const uint32_t pos = warp_append(i < count && !miss, &w.counters[5]);
-        if (i < count && !miss) w.sel[pos] = i;
-        if (!miss) continue;
-        const float4 qo = w.q_o[cur][i], qd = w.q_d[cur][i];
-        const uint32_t p = __float_as_uint(qo.w);
-        const uint64_t g = chunk_start + p;
-        const View<BATCH> vw = view_of<BATCH>(fp, b, w, chunk_start, p);
-        const FrameDev& f = *vw.f;
-        const float4* env = BATCH ? vw.it->env : s.env;
-        const uint32_t env_size = BATCH ? vw.it->env_size : s.env_size;
-        const float4 w4 = w.weight[p];
-        const v3 wold = mk(w4.x, w4.y, w4.z);
-        const float4 col4 = w.radiance[g];
-        v3 color = mk(col4.x, col4.y, col4.z);
-        const v3 emission = (f.pc.use_env_map && env) ? env_lookup(env, env_size, mk(qd.x, qd.y, qd.z))
-                                                       : ld3(f.pc.clear_color) * f.pc.clear_color[3];
-        color = color + emission * wold;
-        w.radiance[g] = make_float4(color.x, color.y, color.z, 0.0f);
-        w.req[p] = 0;
-        if (depth == 0 && vw.g < f.npix) { // sample 0 of the first bounce
-            const uint32_t pix = (uint32_t)vw.g;
-            (BATCH ? vw.it->depth : w.depth)[pix] = 0.0f;
-            uint4* aov_seg = BATCH ? vw.it->seg : w.seg;
-            if (aov_seg) aov_seg[pix] = make_uint4(kMiss, kMiss, kMiss, 0u);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr uint32_t tile = kMissThreads * kMissPer;
+    for (uint32_t base = blockIdx.x * tile; base < count; base += gridDim.x * tile) {
+        uint32_t hitm = 0, missm = 0, nh = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < kMissPer; ++q) {
+            const uint32_t i = base + threadIdx.x * kMissPer + q;
+            if (i < count) {
+                if (__float_as_uint(w.hit[i].w) == kMiss) {
+                    missm |= 1u << q;
+                } else {
+                    hitm |= 1u << q;
+                    ++nh;
+                }
+            }
         }
+        uint32_t x = nh; // inclusive scan over the warp
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_cnt[warp] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (uint32_t k = 0; k < kMissThreads / 32; ++k) t += s_cnt[k];
+            s_base = t ? atomicAdd(&w.counters[5], t) : 0u;
+        }
+        __syncthreads();
+        uint32_t pos = s_base + x - nh;
+        for (uint32_t k = 0; k < warp; ++k) pos += s_cnt[k];
+        __syncthreads(); // s_cnt and s_base are rewritten by the next tile
+#pragma unroll
+        for (uint32_t q = 0; q < kMissPer; ++q)
+            if (hitm & (1u << q)) w.sel[pos++] = base + threadIdx.x * kMissPer + q;
+#pragma unroll 1
+        for (uint32_t q = 0; q < kMissPer; ++q)
+            if (missm & (1u << q)) miss_path<BATCH>(s, fp, b, w, cur, depth, chunk_start, base + threadIdx.x * kMissPer + q);
     }
 }
 
@@ -1283,9 +1326,9 @@ void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const
 void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                  uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
     if (b.items)
-        k_miss<true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        k_miss<true><<<grid, kMissThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     else
-        k_miss<false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        k_miss<false><<<grid, kMissThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
