@@ -305,23 +305,47 @@ template <bool BATCH> __device__ __forceinline__ uint32_t root_of(const SceneDev
 // ---------------------------------------------------------------------------
 // Ray generation (PathTrace.rgen:30-75).
 // ---------------------------------------------------------------------------
+// Queue order of a sample's pixels: bands of kTileH rows, each cut into kTileW-wide column
+// blocks (narrower at the right edge), a block's pixels row by row — a warp's 32 camera rays
+// cover an 8x4 tile instead of 32 pixels of one row, and stay coherent downstream. idx is the
+// position within the sample, the result the row-major pixel index (a bijection for any size).
+constexpr uint32_t kTileW = 8, kTileH = 4;
+__device__ __forceinline__ uint32_t tiled_pixel(uint32_t idx, uint32_t width, uint32_t height) {
+    const uint32_t band = width * kTileH;
+    const uint32_t rb = idx / band;
+    const uint32_t hb = min(kTileH, height - rb * kTileH);
+    const uint32_t r = idx - rb * band;
+    const uint32_t cb = r / (kTileW * hb);
+    const uint32_t wb = min(kTileW, width - cb * kTileW);
+    const uint32_t k = r - cb * kTileW * hb;
+    return (rb * kTileH + k / wb) * width + cb * kTileW + k % wb;
+}
+
 template <bool BATCH>
 __global__ void k_raygen(const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, uint64_t chunk_start,
                          uint32_t chunk_n) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p == 0) w.counters[0] = chunk_n;
-    if (p >= chunk_n) return;
-    uint64_t g = chunk_start + p;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; // queue position
+    if (j == 0) w.counters[0] = chunk_n;
+    if (j >= chunk_n) return;
+    uint64_t g = chunk_start + j;
+    uint64_t view_start = 0; // global index of the view's first path
     const FrameDev* fsel = fp;
+    uint32_t item = 0;
     if (BATCH) {
-        const uint32_t item = find_item(b, g);
-        w.path_item[p] = (uint16_t)item;
+        item = find_item(b, g);
         fsel = &b.items[item].f;
-        g -= b.items[item].path_start;
+        view_start = b.items[item].path_start;
     }
     const FrameDev& f = *fsel;
+    g -= view_start;
     const uint32_t sample = (uint32_t)(g / f.npix);
-    const uint32_t pix = (uint32_t)(g % f.npix);
+    uint32_t pix = (uint32_t)(g % f.npix);
+    // a sample whose pixels all lie in this chunk is queued in tile order; the path id p
+    // (the index of all per-path state) stays the row-major one
+    const uint64_t row = view_start + (uint64_t)sample * f.npix;
+    if (row >= chunk_start && row + f.npix <= chunk_start + chunk_n) pix = tiled_pixel(pix, f.width, f.height);
+    const uint32_t p = (uint32_t)(row + pix - chunk_start);
+    if (BATCH) w.path_item[p] = (uint16_t)item;
     const uint32_t px = pix % f.width, py = pix / f.width;
     PathKey pk{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
     Stream js;
@@ -364,8 +388,8 @@ __global__ void k_raygen(const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
         const float din[4] = {nd.x, nd.y, nd.z, 0.0f};
         mat4_mul(f.cam.view_inv, din, dir);
     }
-    w.q_o[0][p] = make_float4(origin[0], origin[1], origin[2], __uint_as_float(p));
-    w.q_d[0][p] = make_float4(dir[0], dir[1], dir[2], 0.0f);
+    w.q_o[0][j] = make_float4(origin[0], origin[1], origin[2], __uint_as_float(p));
+    w.q_d[0][j] = make_float4(dir[0], dir[1], dir[2], 0.0f);
     w.weight[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     w.radiance[chunk_start + p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
