@@ -117,7 +117,7 @@ def build_scene(device: int, profile=False, debug=False):
     if "blas_leaf_size" in WORKLOAD:
         cfg.setBlasLeafSize(WORKLOAD["blas_leaf_size"])
     if "dyn_refill_below" in WORKLOAD or "dyn_steps" in WORKLOAD:
-        cfg.setDynamicFetch(WORKLOAD.get("dyn_refill_below", 24), WORKLOAD.get("dyn_steps", 16))
+        cfg.setDynamicFetch(WORKLOAD.get("dyn_refill_below", 16), WORKLOAD.get("dyn_steps", 32))
     r = api.Kuafu(cfg)
     cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
                             level=WORKLOAD["level"], seed=WORKLOAD["seed"])

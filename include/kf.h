@@ -87,9 +87,9 @@ typedef struct kf_config {
     uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order, fastest build); 1: host binned
                                       SAH (default: fewer node visits per ray). Same hits. */
     uint32_t dyn_refill_below;     /* persistent traversal: a warp fetches new rays when fewer
-                                      lanes than this are busy (1..32, default 24) */
+                                      lanes than this are busy (1..32, default 16) */
     uint32_t dyn_steps;            /* ... and runs this many traversal steps between fetches
-                                      (1..64, default 16) */
+                                      (1..64, default 32) */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */

@@ -73,7 +73,7 @@ class Config:
     def setHostOnly(self, flag): self._c.host_only = int(bool(flag))
     def setTraversal(self, mode): self._c.traversal = int(mode)
     def setBvhBuilder(self, mode): self._c.bvh_builder = int(mode)
-    def setDynamicFetch(self, refill_below=24, steps=16):
+    def setDynamicFetch(self, refill_below=16, steps=32):
         self._c.dyn_refill_below, self._c.dyn_steps = int(refill_below), int(steps)
 
 

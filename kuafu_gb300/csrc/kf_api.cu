@@ -204,8 +204,8 @@ KF_API void kf_config_init(kf_config* c) {
     c->host_only = 0;
     c->traversal = 1;
     c->bvh_builder = 1;
-    c->dyn_refill_below = 24;
-    c->dyn_steps = 16;
+    c->dyn_refill_below = 16;
+    c->dyn_steps = 32;
 }
 
 KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {

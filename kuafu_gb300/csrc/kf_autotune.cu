@@ -111,13 +111,13 @@ void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count
         }
     // 3b. persistent traversal: refill threshold and steps between refills
     if (best.traversal == 1) {
-        for (uint32_t rb : {16u, 24u, 28u, 32u}) {
+        for (uint32_t rb : {12u, 16u, 24u, 28u}) {
             if (rb == best.refill_below) continue;
             Knobs k = best;
             k.refill_below = rb;
             consider(k);
         }
-        for (uint32_t ns : {2u, 4u, 8u, 16u}) {
+        for (uint32_t ns : {8u, 16u, 32u}) {
             if (ns == best.steps) continue;
             Knobs k = best;
             k.steps = ns;
