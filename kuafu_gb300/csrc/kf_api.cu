@@ -165,7 +165,13 @@ kf_renderer_s::~kf_renderer_s() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     scenes.clear();
+    if (stream2) {
+        cudaStreamSynchronize(stream2);
+        cudaStreamDestroy(stream2);
+    }
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -227,7 +233,10 @@ KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
             KF_CUDA_CHECK(cudaSetDevice(r->device));
             KF_CUDA_CHECK(cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, r->device));
             KF_CUDA_CHECK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+            KF_CUDA_CHECK(cudaStreamCreateWithFlags(&r->stream2, cudaStreamNonBlocking));
             for (cudaEvent_t& ev : r->ev) KF_CUDA_CHECK(cudaEventCreate(&ev));
+            KF_CUDA_CHECK(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
+            KF_CUDA_CHECK(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
             upload_srgb_thresholds(srgb_threshold_table().data());
         }
         // persistent grids: enough resident warps to hide traversal latency

@@ -190,6 +190,10 @@ struct kf_renderer_s {
     std::string graph_key;
     // events for profiling
     cudaEvent_t ev[8] = {};
+    // second stream of the bounce loop: each bounce's shadow traversal and NEE gather run on
+    // it, beside the next bounce's closest-hit traversal (fork / join events, no timing)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // learned denoiser used by run() when cfg.use_denoiser is set
     kf_denoiser_s* denoiser = nullptr;
     // every denoiser created on this renderer (owned: freed by the renderer's destructor)

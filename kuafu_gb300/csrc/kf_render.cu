@@ -238,10 +238,59 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
 
 } // namespace
 
+// The bounce loop on two streams. Bounce d's shadow traversal and NEE gather (stream2)
+// overlap bounce d+1's closest-hit traversal (stream): they share no buffer — the closest-hit
+// kernel reads the next ray queue and writes hit records, the shadow kernel reads the shadow
+// queue and writes visibility, the gather reads bounce d's queue and adds to the radiance.
+// Everything bounce d+1 writes that bounce d's gather reads (its queue count, the NEE
+// requests, contributions, visibility and radiance of the paths) is written by k_miss /
+// k_shade, which wait for the gather (the join). Counters: [3] / [4] fetch cursors, [2]
+// shadow count, [5] hit count, each zeroed on the stream that uses it next.
+static void enqueue_paths_overlapped(kf_renderer_s* r, const SceneDev& sv, const FrameDev* fd, const BatchDev& b,
+                                     const WaveDev& w, uint32_t max_depth, uint64_t npaths, uint32_t chunk) {
+    cudaStream_t st = r->stream, st2 = r->stream2;
+    const bool dyn = r->cfg.traversal == 1;
+    for (uint64_t start = 0; start < npaths; start += chunk) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, npaths - start);
+        launch_raygen(fd, b, w, start, n, st);
+        int cur = 0;
+        for (uint32_t depth = 0; depth <= max_depth; ++depth) {
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 3, 0, sizeof(uint32_t), st));
+            if (dyn)
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal,
+                                 r->cfg.dyn_refill_below, r->cfg.dyn_steps, st);
+            else
+                launch_extend(sv, fd, b, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
+            if (depth > 0) KF_CUDA_CHECK(cudaStreamWaitEvent(st, r->ev_join, 0)); // previous gather done
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + (cur ^ 1), 0, sizeof(uint32_t), st));
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st));
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 5, 0, sizeof(uint32_t), st));
+            launch_miss(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
+            launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
+            KF_CUDA_CHECK(cudaEventRecord(r->ev_fork, st));
+            KF_CUDA_CHECK(cudaStreamWaitEvent(st2, r->ev_fork, 0));
+            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 4, 0, sizeof(uint32_t), st2));
+            if (dyn)
+                launch_trace_dyn(sv, fd, b, w, cur, depth, start, true, r->grid_dyn_shadow, r->count_traversal,
+                                 r->cfg.dyn_refill_below, r->cfg.dyn_steps, st2);
+            else
+                launch_shadow(sv, b, w, r->grid_extend, r->count_traversal, st2);
+            launch_gather(sv, b, w, cur, start, r->grid_shade, st2);
+            KF_CUDA_CHECK(cudaEventRecord(r->ev_join, st2));
+            cur ^= 1;
+        }
+        KF_CUDA_CHECK(cudaStreamWaitEvent(st, r->ev_join, 0)); // last gather done
+    }
+}
+
 // Records the bounce loop over npaths paths (chunks of `chunk`) into the renderer stream.
 static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* fd, const BatchDev& b,
                           const WaveDev& w, uint32_t max_depth, uint64_t npaths, uint32_t chunk, bool profile) {
     cudaStream_t st = r->stream;
+    if (!profile) {
+        enqueue_paths_overlapped(r, sv, fd, b, w, max_depth, npaths, chunk);
+        return;
+    }
     for (uint64_t start = 0; start < npaths; start += chunk) {
         const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, npaths - start);
         launch_raygen(fd, b, w, start, n, st);
