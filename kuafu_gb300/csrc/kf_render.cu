@@ -203,6 +203,7 @@ void ensure_wave(kf_renderer_s* r, uint32_t chunk, uint32_t slots, uint64_t npat
     }
     if (r->cfg.debug_outputs && W.primary.count < npaths) W.primary.resize(npaths, st);
     if (W.counters.count == 0) W.counters.resize(8, st);
+    if (W.scount.count == 0) W.scount.resize(64, st);
     if (W.stats.count == 0) {
         W.stats.resize(16, st);
         KF_CUDA_CHECK(cudaMemsetAsync(W.stats.ptr, 0, W.stats.bytes(), st));
@@ -218,6 +219,8 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
     w.hit = W.hit.ptr;
     w.hit_prim = W.hit_prim.ptr;
     w.sel = W.sel.ptr;
+    w.scount = W.scount.ptr;
+    w.nslot = W.slot_cap;
     w.weight = W.weight.ptr;
     w.nee_w = W.nee_w.ptr;
     w.req = W.req.ptr;
@@ -263,7 +266,7 @@ static void enqueue_paths_overlapped(kf_renderer_s* r, const SceneDev& sv, const
                 launch_extend(sv, fd, b, w, cur, depth, start, r->grid_extend, r->count_traversal, st);
             if (depth > 0) KF_CUDA_CHECK(cudaStreamWaitEvent(st, r->ev_join, 0)); // previous gather done
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + (cur ^ 1), 0, sizeof(uint32_t), st));
-            KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, sizeof(uint32_t), st));
+            KF_CUDA_CHECK(cudaMemsetAsync(w.scount, 0, w.nslot * sizeof(uint32_t), st));
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 5, 0, sizeof(uint32_t), st));
             launch_miss(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
@@ -300,6 +303,7 @@ static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* 
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + (cur ^ 1), 0, sizeof(uint32_t), st));
             // [2] shadow queue count, [3] / [4] dynamic-fetch cursors, [5] rays that hit
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 2, 0, 4 * sizeof(uint32_t), st));
+            KF_CUDA_CHECK(cudaMemsetAsync(w.scount, 0, w.nslot * sizeof(uint32_t), st));
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[0], st));
             if (dyn)
                 launch_trace_dyn(sv, fd, b, w, cur, depth, start, false, r->grid_dyn, r->count_traversal,

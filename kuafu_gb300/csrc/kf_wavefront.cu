@@ -1053,10 +1053,13 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
                        light_sample(s, ItemLights{vw.it}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
             else
                 emit = is_mat && light_sample(s, SceneLights{s}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
-            const uint32_t pos = warp_append(emit, &w.counters[2]);
+            // each light slot has its own shadow queue, so a shadow-traversal warp takes rays
+            // towards one light from neighbouring points
+            const uint32_t pos = warp_append(emit, &w.scount[j]);
             if (emit) {
-                w.sq_o[pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
-                w.sq_d[pos] = make_float4(Ls.x, Ls.y, Ls.z, __uint_as_float((j << 26) | p));
+                const size_t q = (size_t)j * w.chunk_cap + pos;
+                w.sq_o[q] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
+                w.sq_d[q] = make_float4(Ls.x, Ls.y, Ls.z, __uint_as_float((j << 26) | p));
                 w.contrib[(size_t)j * w.chunk_cap + p] = make_float4(c.x, c.y, c.z, 0.0f);
                 w.vis[(size_t)j * w.chunk_cap + p] = 0;
                 req |= 1ull << j;
@@ -1078,14 +1081,40 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
 // ---------------------------------------------------------------------------
 // Shadow rays: any hit in [0.001, tmax] (rchit:175-200, PathTraceShadow.rmiss).
 // ---------------------------------------------------------------------------
+// Shadow queues: slot j's rays are sq_o / sq_d[j * chunk_cap + k], k < scount[j]. Kernels
+// number the rays slot after slot; shadow_prefix puts the prefix sums of the counts in
+// shared memory (all threads of the block must call it) and returns the total.
+constexpr uint32_t kMaxSlots = 64;
+static_assert(1 + KF_MAX_POINT_LIGHTS + KF_MAX_ACTIVE_LIGHTS <= kMaxSlots, "light slots exceed the shadow queues");
+__device__ __forceinline__ uint32_t shadow_prefix(const WaveDev& w, uint32_t* s_pre) {
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t j = 0; j < w.nslot; ++j) {
+            s_pre[j] = t;
+            t += w.scount[j];
+        }
+        s_pre[w.nslot] = t;
+    }
+    __syncthreads();
+    return s_pre[w.nslot];
+}
+// Queue entry of shadow ray i (i < the total).
+__device__ __forceinline__ uint32_t shadow_entry(const WaveDev& w, const uint32_t* s_pre, uint32_t i) {
+    uint32_t j = 0;
+    while (i >= s_pre[j + 1]) ++j;
+    return j * w.chunk_cap + (i - s_pre[j]);
+}
+
 template <bool COUNT, bool BATCH>
 __global__ void __launch_bounds__(128) k_shadow(SceneDev s, BatchDev b, WaveDev w) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
-    const uint32_t count = w.counters[2];
+    __shared__ uint32_t s_pre[kMaxSlots + 1];
+    const uint32_t count = shadow_prefix(w, s_pre);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.stats[2], (unsigned long long)count);
     TraceCounters cnt{0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const float4 o = w.sq_o[i], d = w.sq_d[i];
+        const uint32_t e = shadow_entry(w, s_pre, i);
+        const float4 o = w.sq_o[e], d = w.sq_d[e];
         const uint32_t tag = __float_as_uint(d.w);
         const uint32_t slot = tag >> 26, p = tag & ((1u << 26) - 1u);
         const uint32_t root = BATCH ? b.items[w.path_item[p]].root : (s.has_tlas ? 0u : kNoRoot);
@@ -1117,7 +1146,8 @@ __global__ void __launch_bounds__(128, SHADOW ? 8 : 7)
     k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, int cur, uint32_t depth,
                 uint64_t chunk_start, uint32_t refill_below, int steps) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
-    const uint32_t count = SHADOW ? w.counters[2] : w.counters[cur];
+    __shared__ uint32_t s_pre[SHADOW ? kMaxSlots + 1 : 1];
+    const uint32_t count = SHADOW ? shadow_prefix(w, s_pre) : w.counters[cur];
     uint32_t* fetch = w.counters + (SHADOW ? 4 : 3);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         atomicAdd(&w.stats[SHADOW ? 2 : (depth == 0 ? 0 : 1)], (unsigned long long)count);
@@ -1145,9 +1175,9 @@ __global__ void __launch_bounds__(128, SHADOW ? 8 : 7)
             if (need) {
                 const uint32_t j = base + __popc(m & lanemask_lt());
                 if (j < count) {
-                    idx = j;
+                    idx = SHADOW ? shadow_entry(w, s_pre, j) : j;
                     if (SHADOW) {
-                        const float4 o = w.sq_o[j], d = w.sq_d[j];
+                        const float4 o = w.sq_o[idx], d = w.sq_d[idx];
                         const uint32_t p = __float_as_uint(d.w) & ((1u << 26) - 1u);
                         const uint32_t root = BATCH ? b.items[w.path_item[p]].root : single_root;
                         t.init(root, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, o.w);

@@ -90,6 +90,8 @@ struct WaveDev {
     float4* hit;          // t, u, v, instance bits
     uint32_t* hit_prim;
     uint32_t* sel;        // queue positions of this bounce's rays that hit ([5] of them)
+    uint32_t* scount;     // per light slot j: shadow rays queued, at sq_o/sq_d[j * chunk_cap + k]
+    uint32_t nslot;       // light slots with a shadow queue (scount entries)
     float4* weight;       // throughput carried to the next bounce
     float4* nee_w;        // throughput that scales this bounce's NEE
     uint64_t* req;        // shadow slots requested this bounce (bit j = slot j)
