@@ -198,7 +198,10 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         KF_REQUIRE(nt < (1ull << 26), KF_ERR_LIMIT, "a scene holds at most 67108863 triangles");
         KF_REQUIRE(r->cfg.blas_leaf_size >= 1 && r->cfg.blas_leaf_size <= 16, KF_ERR_INVALID_ARGUMENT,
                    "blas_leaf_size must be in [1, 16]");
-        KF_REQUIRE(s->instances.size() < (1ull << 30), KF_ERR_LIMIT, "too many instances");
+        // TLAS leaves are stack entries too: 26-bit offsets into the leaf list, <= 16 instances
+        KF_REQUIRE(s->instances.size() < (1ull << 26), KF_ERR_LIMIT, "too many instances");
+        KF_REQUIRE(r->cfg.tlas_leaf_size >= 1 && r->cfg.tlas_leaf_size <= 16, KF_ERR_INVALID_ARGUMENT,
+                   "tlas_leaf_size must be in [1, 16]");
         size_t vo = 0, to = 0;
         for (size_t gi = 0; gi < ng; ++gi) {
             const kf_geometry_s* g = s->geometries[gi];
@@ -594,6 +597,9 @@ void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes) {
     B.verts.resize(std::max<size_t>(nv, 1), st);
     B.indices.resize(std::max<size_t>(ni, 1), st);
     B.matidx.resize(std::max<size_t>(nt, 1), st);
+    // traversal stack entries hold 26-bit triangle and TLAS-leaf offsets
+    KF_REQUIRE(nt < (1ull << 26) && nti < (1ull << 26), KF_ERR_LIMIT,
+               "a batch holds at most 67108863 triangles and instances");
     B.tris.resize(std::max<size_t>(nt, 1), st);
     B.geom.resize(std::max<size_t>(ng, 1), st);
     B.inst.resize(std::max<size_t>(ninst, 1), st);

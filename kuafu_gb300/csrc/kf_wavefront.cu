@@ -128,6 +128,15 @@ template <bool SHADOW, bool COUNT> struct Tracer {
             if (sp <= 0) return true;
             e = stack.get(--sp); // below a return entry: a TLAS node or an instance entry
         }
+        if ((e & 0xC0000000u) == kLeafTag && !in_blas) {
+            // a TLAS leaf (instances first .. first + n - 1 of the leaf list): the first
+            // instance is entered in this step, the others wait on the stack
+            const uint32_t first = e & 0x03FFFFFFu;
+#pragma unroll 1
+            for (uint32_t q = (e >> 26) & 0xFu; q > 0; --q)
+                if (sp < kStack) stack.put(sp++, kInstTag | __ldg(s.tlas_inst + first + q));
+            e = kInstTag | __ldg(s.tlas_inst + first);
+        }
         if ((e & 0xC0000000u) == kLeafTag) {
             const uint32_t first = e & 0x03FFFFFFu, cnt_tri = ((e >> 26) & 0xFu) + 1u;
 #pragma unroll 1
@@ -172,29 +181,17 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         if (COUNT) cnt.nodes++;
         float tn[4];
         const int mask = box4(r, n, tmin, best, tn);
-        // children to visit, as (entry distance, stack entry); misses get -inf
+        // children to visit, as (entry distance, stack entry); misses get -inf. A leaf child
+        // (triangles in a BLAS, instances in the TLAS) becomes a leaf entry, sorted with the
+        // inner children by distance.
         float it[4];
         uint32_t ic[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const int cn = lanei(n.cnt, c);
             const uint32_t ch = (uint32_t)lanei(n.child, c);
-            const bool hit = (mask >> c) & 1;
-            it[c] = __int_as_float(0xff800000);
-            ic[c] = 0;
-            if (hit && cn == 0) {
-                it[c] = tn[c];
-                ic[c] = ch;
-            } else if (hit && cn > 0) {
-                if (in_blas) {
-                    it[c] = tn[c];
-                    ic[c] = kLeafTag | ((uint32_t)(cn - 1) << 26) | ch;
-                } else {
-#pragma unroll 1
-                    for (int q = 0; q < cn; ++q)
-                        if (sp < kStack) stack.put(sp++, kInstTag | __ldg(s.tlas_inst + ch + q));
-                }
-            }
+            it[c] = (((mask >> c) & 1) && cn >= 0) ? tn[c] : __int_as_float(0xff800000);
+            ic[c] = cn > 0 ? (kLeafTag | ((uint32_t)(cn - 1) << 26) | ch) : ch;
         }
         // sort by entry distance (fixed network, registers only), then push. Closest-hit rays
         // sort descending, so the nearest child ends on top of the stack; shadow rays (ended by
