@@ -81,6 +81,35 @@ struct TStack {
 // Resumable two-level traversal state: init() then step() until it returns true.
 // One step processes one stack entry (a node with its leaf children, an instance
 // entry or the return to the TLAS), so a warp can interleave rays step by step.
+// The slab test of box4 on a node read in place: the near and far planes of each axis are
+// loaded by the ray's direction signs (no selects), with the child links.
+__device__ __forceinline__ int box4_dir(const PRay& r, const float4* p, float tmin, float tmax, float tn_out[4],
+                                        int4& child, int4& cnt) {
+    const int sx = r.ix >= 0.0f ? 0 : 1, sy = r.iy >= 0.0f ? 0 : 1, sz = r.iz >= 0.0f ? 0 : 1;
+    const float4 nx = __ldg(p + sx), fx = __ldg(p + (1 - sx));
+    const float4 ny = __ldg(p + 2 + sy), fy = __ldg(p + (3 - sy));
+    const float4 nz = __ldg(p + 4 + sz), fz = __ldg(p + (5 - sz));
+    child = __ldg(reinterpret_cast<const int4*>(p + 6));
+    cnt = __ldg(reinterpret_cast<const int4*>(p + 7));
+    int mask = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float t1x, t1y, t1z;
+        const float t0x = slab1(lane(nx, c), lane(fx, c), r.ox, r.ix, t1x);
+        const float t0y = slab1(lane(ny, c), lane(fy, c), r.oy, r.iy, t1y);
+        const float t0z = slab1(lane(nz, c), lane(fz, c), r.oz, r.iz, t1z);
+        float tn = fmaxf(tmin, t0x);
+        float tf = fminf(__int_as_float(0x7f800000), t1x);
+        tn = fmaxf(tn, t0y);
+        tf = fminf(tf, t1y);
+        tn = fmaxf(tn, t0z);
+        tf = fminf(tf, t1z);
+        tn_out[c] = tn;
+        if (tn <= fminf(tf * KF_BOX_WIDEN, tmax)) mask |= 1 << c;
+    }
+    return mask;
+}
+
 template <bool SHADOW, bool COUNT> struct Tracer {
     PRay wr, r;
     TStack stack;
@@ -177,10 +206,11 @@ template <bool SHADOW, bool COUNT> struct Tracer {
             stack.put(sp++, kPopTag);
             e = meta.x; // the BLAS root, visited in this step
         }
-        const Node4 n = load_node(in_blas ? s.blas_nodes : s.tlas_nodes, e);
-        if (COUNT) cnt.nodes++;
+        Node4 n;
         float tn[4];
-        const int mask = box4(r, n, tmin, best, tn);
+        const int mask = box4_dir(r, reinterpret_cast<const float4*>((in_blas ? s.blas_nodes : s.tlas_nodes) + e), tmin,
+                                  best, tn, n.child, n.cnt);
+        if (COUNT) cnt.nodes++;
         // children to visit, as (entry distance, stack entry); misses get -inf. A leaf child
         // (triangles in a BLAS, instances in the TLAS) becomes a leaf entry, sorted with the
         // inner children by distance.
@@ -213,8 +243,20 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         KF_CSWAP(1, 2)
 #undef KF_CSWAP
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
-            if (it[c] != __int_as_float(0xff800000) && sp < kStack) stack.put(sp++, ic[c]);
+        if (sp + 4 <= kSmemStack) { // all four fit the shared part of the stack
+            uint32_t* top = stack.sm + sp * kThreadsTrace;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (it[c] != __int_as_float(0xff800000)) {
+                    *top = ic[c];
+                    top += kThreadsTrace;
+                    ++sp;
+                }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (it[c] != __int_as_float(0xff800000) && sp < kStack) stack.put(sp++, ic[c]);
+        }
         return sp <= 0;
     }
 };
@@ -1136,10 +1178,10 @@ __global__ void __launch_bounds__(128) k_shadow(SceneDev s, BatchDev b, WaveDev 
 // ---------------------------------------------------------------------------
 // refill_below: a warp fetches rays when fewer lanes than this are busy; steps: traversal
 // steps between fetches (both tunable, kf_config.dyn_refill_below / dyn_steps).
-// Occupancy: 7 resident blocks per SM for closest-hit rays (72 registers, a few bytes of
-// spill) and 8 for shadow rays (64 registers) measured fastest on the 256-icosphere frame.
+// Occupancy: 7 resident blocks per SM for closest-hit rays (72 registers, 2 bytes of spill)
+// and 9 for shadow rays (56 registers, no spill) measured fastest on the 256-icosphere frame.
 template <bool SHADOW, bool COUNT, bool BATCH>
-__global__ void __launch_bounds__(128, SHADOW ? 8 : 7)
+__global__ void __launch_bounds__(128, SHADOW ? 9 : 7)
     k_trace_dyn(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w, int cur, uint32_t depth,
                 uint64_t chunk_start, uint32_t refill_below, int steps) {
     __shared__ uint32_t s_stack[kSmemStack * kThreadsTrace];
