@@ -154,7 +154,7 @@ struct BatchState {
 
 // Wavefront buffers sized for one chunk of paths.
 struct WaveBuffers {
-    kf::DeviceBuffer<float4> q_o0, q_o1, q_d0, q_d1, hit, weight, nee_w, contrib, sq_o, sq_d;
+    kf::DeviceBuffer<float4> q_o0, q_o1, q_d0, q_d1, hit, weight, nee_w, nee_in, contrib, sq_o, sq_d;
     kf::DeviceBuffer<uint32_t> counters, hit_prim, sel, scount;
     kf::DeviceBuffer<uint64_t> req;
     kf::DeviceBuffer<uint8_t> vis;

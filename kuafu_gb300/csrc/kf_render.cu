@@ -184,7 +184,7 @@ void ensure_wave(kf_renderer_s* r, uint32_t chunk, uint32_t slots, uint64_t npat
         W.q_o0.resize(chunk, st); W.q_o1.resize(chunk, st);
         W.q_d0.resize(chunk, st); W.q_d1.resize(chunk, st);
         W.hit.resize(chunk, st); W.hit_prim.resize(chunk, st); W.sel.resize(chunk, st);
-        W.weight.resize(chunk, st); W.nee_w.resize(chunk, st);
+        W.weight.resize(chunk, st); W.nee_w.resize(chunk, st); W.nee_in.resize((size_t)6 * chunk, st);
         W.req.resize(chunk, st);
         W.chunk_cap = chunk;
         W.slot_cap = 0;
@@ -223,6 +223,7 @@ WaveDev wave_view(kf_renderer_s* r, kf_camera_s* c) {
     w.nslot = W.slot_cap;
     w.weight = W.weight.ptr;
     w.nee_w = W.nee_w.ptr;
+    w.nee_in = W.nee_in.ptr;
     w.req = W.req.ptr;
     w.contrib = W.contrib.ptr;
     w.vis = W.vis.ptr;
@@ -270,6 +271,7 @@ static void enqueue_paths_overlapped(kf_renderer_s* r, const SceneDev& sv, const
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 5, 0, sizeof(uint32_t), st));
             launch_miss(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
+            launch_nee(sv, fd, b, w, depth, start, r->grid_shade, st);
             KF_CUDA_CHECK(cudaEventRecord(r->ev_fork, st));
             KF_CUDA_CHECK(cudaStreamWaitEvent(st2, r->ev_fork, 0));
             KF_CUDA_CHECK(cudaMemsetAsync(w.counters + 4, 0, sizeof(uint32_t), st2));
@@ -313,6 +315,7 @@ static void enqueue_paths(kf_renderer_s* r, const SceneDev& sv, const FrameDev* 
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[1], st));
             launch_miss(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
             launch_shade(sv, fd, b, w, cur, depth, start, r->grid_shade, st);
+            launch_nee(sv, fd, b, w, depth, start, r->grid_shade, st);
             if (profile) KF_CUDA_CHECK(cudaEventRecord(r->ev[2], st));
             if (dyn)
                 launch_trace_dyn(sv, fd, b, w, cur, depth, start, true, r->grid_dyn_shadow, r->count_traversal,

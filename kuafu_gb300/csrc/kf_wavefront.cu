@@ -1079,7 +1079,70 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
                 }
             }
         }
-        // light slots: one warp-uniform loop, one ballot per slot
+        // what the light samples of this hit need, for k_nee (hit-list order)
+        if (valid) {
+            float4* rec = w.nee_in + (size_t)6 * (base + lane);
+            rec[0] = make_float4(worldPos.x, worldPos.y, worldPos.z,
+                                 __uint_as_float(p | (is_mat ? 0x80000000u : 0u) | (sh.isInside ? 0x40000000u : 0u)));
+            rec[1] = make_float4(N.x, N.y, N.z, sh.f);
+            rec[2] = make_float4(V.x, V.y, V.z, sh.a2);
+            rec[3] = make_float4(sh.diffuseColor.x, sh.diffuseColor.y, sh.diffuseColor.z, wnew.x);
+            rec[4] = make_float4(sh.specularColor.x, sh.specularColor.y, sh.specularColor.z, wnew.y);
+            rec[5] = make_float4(sh.transmissionColor.x, sh.transmissionColor.y, sh.transmissionColor.z, wnew.z);
+        }
+        const uint32_t pos = warp_append(cont, &w.counters[nxt]);
+        if (cont) {
+            w.q_o[nxt][pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, __uint_as_float(p));
+            w.q_d[nxt][pos] = make_float4(L.x, L.y, L.z, 0.0f);
+            w.weight[p] = make_float4(wcont.x, wcont.y, wcont.z, 0.0f);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Light samples of the hits (traceDirectionalLight / tracePointLights / traceActiveLights,
+// rchit:204-316, after the BSDF sample as in rchit:457-460): one warp-uniform loop over the
+// light slots, one ballot per slot. A kernel of its own, beside k_shade: each of the two is
+// small enough for the instruction cache.
+// ---------------------------------------------------------------------------
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+                                             uint32_t depth, uint64_t chunk_start) {
+    const uint32_t count = w.counters[5];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count; base += stride) {
+        const bool valid = base + lane < count;
+        uint32_t p = 0;
+        bool is_mat = false;
+        v3 worldPos = splat(0.0f), N = splat(0.0f), V = splat(0.0f), wnew = splat(0.0f);
+        Shading sh;
+        sh.f = 1.0f; sh.a2 = 0.0f;
+        sh.diffuseColor = sh.specularColor = sh.transmissionColor = splat(0.0f);
+        sh.isInside = false;
+        View<BATCH> vw{fp, nullptr, 0};
+        PathKey pk{make_uint2(0, 0), 0, 0};
+        if (valid) {
+            const float4* rec = w.nee_in + (size_t)6 * (base + lane);
+            const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3], r4 = rec[4], r5 = rec[5];
+            const uint32_t bits = __float_as_uint(r0.w);
+            p = bits & 0x3FFFFFFFu;
+            is_mat = (bits & 0x80000000u) != 0;
+            sh.isInside = (bits & 0x40000000u) != 0;
+            worldPos = mk(r0.x, r0.y, r0.z);
+            N = mk(r1.x, r1.y, r1.z);
+            sh.f = r1.w;
+            V = mk(r2.x, r2.y, r2.z);
+            sh.a2 = r2.w;
+            sh.diffuseColor = mk(r3.x, r3.y, r3.z);
+            sh.specularColor = mk(r4.x, r4.y, r4.z);
+            sh.transmissionColor = mk(r5.x, r5.y, r5.z);
+            wnew = mk(r3.w, r4.w, r5.w);
+            vw = view_of<BATCH>(fp, b, w, chunk_start, p);
+            const FrameDev& f = *vw.f;
+            pk = PathKey{make_uint2(f.seed ^ (uint32_t)(vw.g % f.npix), f.camera_index), (uint32_t)(vw.g / f.npix),
+                         f.frame};
+        }
         uint64_t req = 0;
         const uint32_t nslots =
             BATCH ? __reduce_max_sync(kFull, valid ? vw.it->num_slots : 0u) : s.num_slots;
@@ -1107,12 +1170,6 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
         if (valid) {
             w.req[p] = req;
             if (req) w.nee_w[p] = make_float4(wnew.x, wnew.y, wnew.z, 0.0f);
-        }
-        const uint32_t pos = warp_append(cont, &w.counters[nxt]);
-        if (cont) {
-            w.q_o[nxt][pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, __uint_as_float(p));
-            w.q_d[nxt][pos] = make_float4(L.x, L.y, L.z, 0.0f);
-            w.weight[p] = make_float4(wcont.x, wcont.y, wcont.z, 0.0f);
         }
     }
 }
@@ -1423,6 +1480,14 @@ void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const 
         k_miss<true><<<grid, kMissThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     else
         k_miss<false><<<grid, kMissThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+void launch_nee(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, uint32_t depth,
+                uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
+    if (b.items)
+        k_nee<true><<<grid, 128, 0, st>>>(s, f, b, w, depth, chunk_start);
+    else
+        k_nee<false><<<grid, 128, 0, st>>>(s, f, b, w, depth, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,

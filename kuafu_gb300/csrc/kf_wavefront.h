@@ -94,6 +94,7 @@ struct WaveDev {
     uint32_t nslot;       // light slots with a shadow queue (scount entries)
     float4* weight;       // throughput carried to the next bounce
     float4* nee_w;        // throughput that scales this bounce's NEE
+    float4* nee_in;       // per hit (hit-list order), 6 float4: what k_nee needs of k_shade's shading
     uint64_t* req;        // shadow slots requested this bounce (bit j = slot j)
     float4* contrib;      // [slot][chunk] light contribution
     uint8_t* vis;         // [slot][chunk] 1 = unoccluded
@@ -122,6 +123,9 @@ void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const
                   uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st);
 void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                  uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st);
+// Light samples (shadow queues, contributions, NEE requests) of the hits k_shade shaded.
+void launch_nee(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, uint32_t depth,
+                uint64_t chunk_start, uint32_t grid, cudaStream_t st);
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
                    cudaStream_t st);
 // Persistent traversal with dynamic ray fetch (closest hit, or shadow rays when `shadow`).
