@@ -241,7 +241,7 @@ KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {
         }
         // persistent grids: enough resident warps to hide traversal latency
         r->grid_extend = (uint32_t)r->num_sms * 16;
-        r->grid_shade = (uint32_t)r->num_sms * 8;
+        r->grid_shade = (uint32_t)r->num_sms * 16; // 16 blocks per SM measured fastest (4, 8, 16)
         if (!r->cfg.host_only) {
             r->grid_dyn = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm(false);
             r->grid_dyn_shadow = (uint32_t)r->num_sms * trace_dyn_blocks_per_sm(true);
