@@ -500,9 +500,9 @@ def run_ours(args):
             "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WORKLOAD["width"] * WORKLOAD["height"] * 4},
             "clocks": clk,
-            # per frame: raygen; per bounce closest-hit traversal, k_miss, k_shade, shadow
-            # traversal, k_gather; resolve and sRGB
-            "gpu_launches": args.steps * (1 + 5 * (WORKLOAD["depth"] + 1) + 2),
+            # per frame: raygen; per bounce closest-hit traversal, k_miss, k_shade, k_nee,
+            # shadow traversal, k_gather; resolve and sRGB
+            "gpu_launches": args.steps * (1 + 6 * (WORKLOAD["depth"] + 1) + 2),
         }
         if ttr is not None:
             result["time_to_relmse"] = ttr
