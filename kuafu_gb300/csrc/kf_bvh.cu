@@ -304,7 +304,7 @@ __global__ void k_collapse(int n, int max_leaf, const int* __restrict__ left, co
         hx[c] = b.x; hy[c] = b.y; hz[c] = b.z;
         const int rs = range_size(node, n, range);
         if (node >= n - 1 || rs <= max_leaf) {
-            cc[c] = range_first(node, n, range);
+            cc[c] = leaf_child(range_first(node, n, range), rs);
             cn[c] = rs;
         } else {
             const int slot = atomicAdd(node_count, 1);
@@ -341,7 +341,7 @@ __global__ void k_single_leaf(const float4* __restrict__ lo, const float4* __res
     o.hiy = make_float4(b.y, -INFINITY, -INFINITY, -INFINITY);
     o.loz = make_float4(a.z, INFINITY, INFINITY, INFINITY);
     o.hiz = make_float4(b.z, -INFINITY, -INFINITY, -INFINITY);
-    o.child = make_int4(0, 0, 0, 0);
+    o.child = make_int4(leaf_child(0, n), 0, 0, 0);
     o.cnt = make_int4(n, -1, -1, -1);
     out[0] = o;
 }
@@ -658,7 +658,7 @@ int build_wide_bvh_sah_host(const float* lo, const float* hi, int n, int max_lea
             lx[c] = b.box.lo[0]; ly[c] = b.box.lo[1]; lz[c] = b.box.lo[2];
             hx[c] = b.box.hi[0]; hy[c] = b.box.hi[1]; hz[c] = b.box.hi[2];
             if (b.left < 0) {
-                cc[c] = b.first;
+                cc[c] = leaf_child(b.first, b.count);
                 cn[c] = b.count;
             } else {
                 const int slot = (int)out.size();

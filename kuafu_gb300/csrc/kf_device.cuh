@@ -189,13 +189,24 @@ struct Stream {
 
 // 4-wide node, 128 B = 8 x 16-B loads. Child c of the node is described by
 // lane c of every field.  cnt[c] == 0: inner child, child[c] = node index;
-// cnt[c] > 0: leaf with cnt[c] primitives starting at child[c]; cnt[c] < 0: empty.
+// cnt[c] > 0: leaf with cnt[c] primitives starting at primitive f, child[c] =
+// leaf_child(f, cnt[c]) (the traversal's stack entry for it); cnt[c] < 0: empty
+// (inverted box, never hit).
 struct alignas(16) Node4 {
     float4 lox, hix, loy, hiy, loz, hiz;
     int4 child;
     int4 cnt;
 };
 static_assert(sizeof(Node4) == 128, "Node4 must be 128 bytes");
+
+// Leaf child link: bit 30 set, count - 1 (<= 15) in bits 26..29, first primitive in bits
+// 0..25, so that the traversal pushes the link as it is. Rebasing a leaf by a primitive
+// offset is a plain addition (the sum stays below 2^26).
+constexpr uint32_t kLeafChildTag = 0x40000000u, kLeafFirstMask = 0x03FFFFFFu;
+__host__ __device__ __forceinline__ int leaf_child(int first, int count) {
+    return (int)(kLeafChildTag | ((uint32_t)(count - 1) << 26) | (uint32_t)first);
+}
+__host__ __device__ __forceinline__ int leaf_first(int child) { return (int)((uint32_t)child & kLeafFirstMask); }
 
 // TLAS instance record, 64 B: world->object rows + BLAS addressing.
 struct alignas(16) InstanceRec {

@@ -419,7 +419,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
                     hz[c] = std::max(std::max(k.hiz.x, k.hiz.y), std::max(k.hiz.z, k.hiz.w));
                 } else {
                     for (int q = 0; q < cn[c]; ++q) {
-                        const uint32_t id = G.tlas_host_inst[ch[c] + q];
+                        const uint32_t id = G.tlas_host_inst[leaf_first(ch[c]) + q];
                         lx[c] = std::min(lx[c], wlo[id].x); ly[c] = std::min(ly[c], wlo[id].y);
                         lz[c] = std::min(lz[c], wlo[id].z); hx[c] = std::max(hx[c], whi[id].x);
                         hy[c] = std::max(hy[c], whi[id].y); hz[c] = std::max(hz[c], whi[id].z);

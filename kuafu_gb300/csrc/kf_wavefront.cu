@@ -30,6 +30,7 @@ constexpr int kStack = 96;
 constexpr uint32_t kInstTag = 0x80000000u;
 constexpr uint32_t kPopTag = 0xC0000000u;
 constexpr uint32_t kLeafTag = 0x40000000u;
+static_assert(kLeafTag == kLeafChildTag, "leaf child links are pushed as stack entries");
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 struct HitOut {
@@ -211,17 +212,16 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         const int mask = box4_dir(r, reinterpret_cast<const float4*>((in_blas ? s.blas_nodes : s.tlas_nodes) + e), tmin,
                                   best, tn, n.child, n.cnt);
         if (COUNT) cnt.nodes++;
-        // children to visit, as (entry distance, stack entry); misses get -inf. A leaf child
-        // (triangles in a BLAS, instances in the TLAS) becomes a leaf entry, sorted with the
-        // inner children by distance.
+        // children to visit, as (entry distance, stack entry); misses get -inf. The child
+        // links are stack entries already: node indices, and leaf entries (triangles in a
+        // BLAS, instances in the TLAS) sorted with the inner children by distance. Empty
+        // children have inverted boxes and never hit.
         float it[4];
         uint32_t ic[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            const int cn = lanei(n.cnt, c);
-            const uint32_t ch = (uint32_t)lanei(n.child, c);
-            it[c] = (((mask >> c) & 1) && cn >= 0) ? tn[c] : __int_as_float(0xff800000);
-            ic[c] = cn > 0 ? (kLeafTag | ((uint32_t)(cn - 1) << 26) | ch) : ch;
+            it[c] = ((mask >> c) & 1) ? tn[c] : __int_as_float(0xff800000);
+            ic[c] = (uint32_t)lanei(n.child, c);
         }
         // sort by entry distance (fixed network, registers only), then push. Closest-hit rays
         // sort descending, so the nearest child ends on top of the stack; shadow rays (ended by
