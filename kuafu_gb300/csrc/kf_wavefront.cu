@@ -47,16 +47,38 @@ struct TraceCounters {
 // Stochastic alpha of non-opaque geometry (PathTrace.rahit:30-48): a candidate is
 // ignored when alpha == 0 or when a uniform draw exceeds alpha. The draws come from
 // the path's any-hit stream; their order follows the traversal order.
+// The path's Philox key is derived only when a draw is needed (non-opaque geometry is
+// rare): fetching a ray then costs no 64-bit division.
 struct AnyHitCtx {
-    const PathKey* pk;
+    const FrameDev* f; // the path's view
+    uint64_t g;        // the path's index in its view
     Stream st;
 };
+
+// Sample and pixel of path g of a view (sample-major): a 32-bit division whenever g fits
+// in 32 bits (a view below 2^32 paths), the 64-bit one otherwise.
+__device__ __forceinline__ void split_path(uint64_t g, uint32_t npix, uint32_t& sample, uint32_t& pix) {
+    if ((g >> 32) == 0) {
+        const uint32_t g32 = (uint32_t)g;
+        sample = g32 / npix;
+        pix = g32 - sample * npix;
+    } else {
+        sample = (uint32_t)(g / npix);
+        pix = (uint32_t)(g % npix);
+    }
+}
+
+__device__ __forceinline__ PathKey path_key(const FrameDev& f, uint64_t g) {
+    uint32_t sample, pix;
+    split_path(g, f.npix, sample, pix);
+    return PathKey{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
+}
 
 __device__ __forceinline__ bool anyhit_accept(const SceneDev& s, uint32_t geometry, uint32_t prim, AnyHitCtx& ah) {
     const uint4 gi = __ldg(s.geom + geometry);
     const float alpha = s.materials[__ldg(s.matidx + gi.y + prim)].alpha;
     if (alpha == 0.0f) return false;
-    if (ah.pk && ah.st.next(*ah.pk) > alpha) return false;
+    if (ah.st.next(path_key(*ah.f, ah.g)) > alpha) return false;
     return true;
 }
 
@@ -378,8 +400,8 @@ __global__ void k_raygen(const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
     }
     const FrameDev& f = *fsel;
     g -= view_start;
-    const uint32_t sample = (uint32_t)(g / f.npix);
-    uint32_t pix = (uint32_t)(g % f.npix);
+    uint32_t sample, pix;
+    split_path(g, f.npix, sample, pix);
     // a sample whose pixels all lie in this chunk is queued in tile order; the path id p
     // (the index of all per-path state) stays the row-major one
     const uint64_t row = view_start + (uint64_t)sample * f.npix;
@@ -450,12 +472,9 @@ __global__ void __launch_bounds__(128) k_extend(SceneDev s, const FrameDev* __re
         const float4 o = qo[i], d = qd[i];
         HitOut h;
         const View<BATCH> v = view_of<BATCH>(fp, b, w, chunk_start, __float_as_uint(o.w));
-        const uint64_t g = v.g;
-        const uint32_t npix = v.f->npix;
-        const PathKey pk{make_uint2(v.f->seed ^ (uint32_t)(g % npix), v.f->camera_index), (uint32_t)(g / npix),
-                         v.f->frame};
         AnyHitCtx ah;
-        ah.pk = &pk;
+        ah.f = v.f;
+        ah.g = v.g;
         ah.st.init(depth, KF_RNG_ANYHIT);
         trace<false, COUNT>(s, root_of<BATCH>(s, v), s_stack, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX, h,
                             cnt, &ah);
@@ -899,8 +918,8 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
             g = chunk_start + p; // radiance index (the batch's path space)
             vw = view_of<BATCH>(fp, b, w, chunk_start, p);
             const FrameDev& f = *vw.f;
-            const uint32_t sample = (uint32_t)(vw.g / f.npix);
-            const uint32_t pix = (uint32_t)(vw.g % f.npix);
+            uint32_t sample, pix;
+            split_path(vw.g, f.npix, sample, pix);
             pk = PathKey{make_uint2(f.seed ^ pix, f.camera_index), sample, f.frame};
             float4* aov_albedo = BATCH ? vw.it->albedo : w.albedo;
             float4* aov_normal = BATCH ? vw.it->normal : w.normal;
@@ -1140,8 +1159,7 @@ __global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restr
             wnew = mk(r3.w, r4.w, r5.w);
             vw = view_of<BATCH>(fp, b, w, chunk_start, p);
             const FrameDev& f = *vw.f;
-            pk = PathKey{make_uint2(f.seed ^ (uint32_t)(vw.g % f.npix), f.camera_index), (uint32_t)(vw.g / f.npix),
-                         f.frame};
+            pk = path_key(f, vw.g);
         }
         uint64_t req = 0;
         const uint32_t nslots =
@@ -1252,9 +1270,9 @@ __global__ void __launch_bounds__(128, SHADOW ? 9 : 7)
     Tracer<SHADOW, COUNT> t;
     t.stack.sm = s_stack + threadIdx.x;
     t.cnt = TraceCounters{0, 0, 0};
-    PathKey pk{make_uint2(0, 0), 0, 0};
     AnyHitCtx ah;
-    ah.pk = &pk;
+    ah.f = fp;
+    ah.g = 0;
     ah.st.init(depth, KF_RNG_ANYHIT);
     bool active = false;
     bool exhausted = false;
@@ -1280,9 +1298,8 @@ __global__ void __launch_bounds__(128, SHADOW ? 9 : 7)
                     } else {
                         const float4 o = w.q_o[cur][j], d = w.q_d[cur][j];
                         const View<BATCH> v = view_of<BATCH>(fp, b, w, chunk_start, __float_as_uint(o.w));
-                        const uint32_t npix = v.f->npix;
-                        pk = PathKey{make_uint2(v.f->seed ^ (uint32_t)(v.g % npix), v.f->camera_index),
-                                     (uint32_t)(v.g / npix), v.f->frame};
+                        ah.f = v.f;
+                        ah.g = v.g;
                         ah.st.init(depth, KF_RNG_ANYHIT);
                         t.init(BATCH ? v.it->root : single_root, o.x, o.y, o.z, d.x, d.y, d.z, KF_T_MIN, KF_T_MAX);
                     }
