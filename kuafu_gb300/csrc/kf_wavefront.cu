@@ -264,7 +264,6 @@ template <bool SHADOW, bool COUNT> struct Tracer {
         KF_CSWAP(1, 3)
         KF_CSWAP(1, 2)
 #undef KF_CSWAP
-#pragma unroll
         if (sp + 4 <= kSmemStack) { // all four fit the shared part of the stack
             uint32_t* top = stack.sm + sp * kThreadsTrace;
 #pragma unroll
@@ -696,7 +695,6 @@ __device__ v3 calcDirectContribution(Stream& st, const PathKey& pk, v3 L, v3 V, 
 // Light slots of a view: the scene's own (single-view frame) or its item's (batched).
 struct SceneLights {
     const SceneDev& s;
-    __device__ __forceinline__ uint32_t num() const { return s.num_slots; }
     __device__ __forceinline__ uint32_t group(uint32_t j) const { return s.slot_group[j]; }
     __device__ __forceinline__ uint32_t index(uint32_t j) const { return s.slot_index[j]; }
     __device__ __forceinline__ const kf_dir_light_ubo* dlight() const { return s.dlight; }
@@ -705,7 +703,6 @@ struct SceneLights {
 };
 struct ItemLights {
     const ItemDev* it;
-    __device__ __forceinline__ uint32_t num() const { return it->num_slots; }
     __device__ __forceinline__ uint32_t group(uint32_t j) const { return it->slot_group[j]; }
     __device__ __forceinline__ uint32_t index(uint32_t j) const { return it->slot_index[j]; }
     __device__ __forceinline__ const kf_dir_light_ubo* dlight() const { return it->dlight; }
