@@ -400,11 +400,21 @@ __global__ void k_raygen(const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
     const FrameDev& f = *fsel;
     g -= view_start;
     uint32_t sample, pix;
-    split_path(g, f.npix, sample, pix);
-    // a sample whose pixels all lie in this chunk is queued in tile order; the path id p
-    // (the index of all per-path state) stays the row-major one
+    if (view_start >= chunk_start && view_start + (uint64_t)f.npix * f.pc.spp <= chunk_start + chunk_n) {
+        // the whole view in this chunk: a pixel's samples are queued one after the other,
+        // pixels in tile order, so a warp's camera rays start in 4 neighbouring pixels
+        // (+5 % over queuing each sample's pixels in tile order)
+        uint32_t t;
+        split_path(g, f.pc.spp, t, sample);
+        pix = tiled_pixel(t, f.width, f.height);
+    } else {
+        split_path(g, f.npix, sample, pix);
+        // a sample whose pixels all lie in this chunk is queued in tile order
+        const uint64_t row0 = view_start + (uint64_t)sample * f.npix;
+        if (row0 >= chunk_start && row0 + f.npix <= chunk_start + chunk_n) pix = tiled_pixel(pix, f.width, f.height);
+    }
+    // the path id p (the index of all per-path state) stays the row-major one
     const uint64_t row = view_start + (uint64_t)sample * f.npix;
-    if (row >= chunk_start && row + f.npix <= chunk_start + chunk_n) pix = tiled_pixel(pix, f.width, f.height);
     const uint32_t p = (uint32_t)(row + pix - chunk_start);
     if (BATCH) w.path_item[p] = (uint16_t)item;
     const uint32_t px = pix % f.width, py = pix / f.width;
