@@ -903,9 +903,12 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
                                                int cur, uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[5]; // rays of this bounce that hit (k_miss takes the others)
     const int nxt = cur ^ 1;
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count; base += stride) {
+    __shared__ uint32_t s_cnt[2][4], s_base[2]; // per tile parity: the block scan of continuing paths
+    uint32_t par = 0;
+    for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < count; bbase += stride, par ^= 1) {
+        const uint32_t base = bbase + (threadIdx.x & ~31u);
         const bool valid = base + lane < count;
         const uint32_t i = valid ? w.sel[base + lane] : 0u; // queue position of the ray
         uint32_t p = 0;
@@ -1116,7 +1119,17 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
             rec[4] = make_float4(sh.specularColor.x, sh.specularColor.y, sh.specularColor.z, wnew.y);
             rec[5] = make_float4(sh.transmissionColor.x, sh.transmissionColor.y, sh.transmissionColor.z, wnew.z);
         }
-        const uint32_t pos = warp_append(cont, &w.counters[nxt]);
+        // next rays in hit-list order: one atomic per block tile
+        const uint32_t m = __ballot_sync(kFull, cont);
+        if (lane == 0) s_cnt[par][wid] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t t = s_cnt[par][0] + s_cnt[par][1] + s_cnt[par][2] + s_cnt[par][3];
+            s_base[par] = t ? atomicAdd(&w.counters[nxt], t) : 0u;
+        }
+        __syncthreads();
+        uint32_t pos = s_base[par] + __popc(m & lanemask_lt());
+        for (uint32_t k = 0; k < wid; ++k) pos += s_cnt[par][k];
         if (cont) {
             w.q_o[nxt][pos] = make_float4(worldPos.x, worldPos.y, worldPos.z, __uint_as_float(p));
             w.q_d[nxt][pos] = make_float4(L.x, L.y, L.z, 0.0f);
@@ -1135,9 +1148,12 @@ template <bool BATCH>
 __global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                              uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[5];
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count; base += stride) {
+    __shared__ uint32_t s_cnt[2][4], s_base[2]; // per slot parity: the block scan of emitted rays
+    uint32_t par = 0;
+    for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < count; bbase += stride) {
+        const uint32_t base = bbase + (threadIdx.x & ~31u);
         const bool valid = base + lane < count;
         uint32_t p = 0;
         bool is_mat = false;
@@ -1182,7 +1198,22 @@ __global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restr
                 emit = is_mat && light_sample(s, SceneLights{s}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
             // each light slot has its own shadow queue, so a shadow-traversal warp takes rays
             // towards one light from neighbouring points
-            const uint32_t pos = warp_append(emit, &w.scount[j]);
+            uint32_t pos;
+            if (BATCH) { // slot counts differ between the warps of a block
+                pos = warp_append(emit, &w.scount[j]);
+            } else {
+                const uint32_t m = __ballot_sync(kFull, emit);
+                if (lane == 0) s_cnt[par][wid] = __popc(m);
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    const uint32_t t = s_cnt[par][0] + s_cnt[par][1] + s_cnt[par][2] + s_cnt[par][3];
+                    s_base[par] = t ? atomicAdd(&w.scount[j], t) : 0u;
+                }
+                __syncthreads();
+                pos = s_base[par] + __popc(m & lanemask_lt());
+                for (uint32_t k = 0; k < wid; ++k) pos += s_cnt[par][k];
+                par ^= 1;
+            }
             if (emit) {
                 const size_t q = (size_t)j * w.chunk_cap + pos;
                 w.sq_o[q] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
