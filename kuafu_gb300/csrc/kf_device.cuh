@@ -255,10 +255,10 @@ KF_DEV void prep_ray(PRay& r) {
     r.kz = kz;
     r.Sx = comp(r.dx, r.dy, r.dz, kx) / dkz;
     r.Sy = comp(r.dx, r.dy, r.dz, ky) / dkz;
-    r.Sz = 1.0f / dkz;
     r.ix = 1.0f / r.dx;
     r.iy = 1.0f / r.dy;
     r.iz = 1.0f / r.dz;
+    r.Sz = comp(r.ix, r.iy, r.iz, kz); // = 1 / dkz, the same correctly rounded quotient
 }
 
 // World -> object transform of a ray: o' = W2O (o, 1), d' = W2O (d, 0).
