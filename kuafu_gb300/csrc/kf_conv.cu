@@ -32,7 +32,6 @@ __device__ uint32_t g_tc_error;
 
 namespace {
 
-constexpr int kStages = 4;
 constexpr long long kWaitBudget = 2000000000ll; // SM cycles (~1 s)
 
 struct TcParams {
@@ -55,7 +54,7 @@ struct TcParams {
 __device__ __forceinline__ void set_error(uint32_t code) { atomicCAS(&g_tc_error, 0u, code); }
 
 // MODE 0: implicit conv3x3 (4D A, 3D B); MODE 1: GEMM (2D A, 2D B).
-template <int MODE, int SWZ>
+template <int MODE, int SWZ, int kStages>
 __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorMap tmA,
                                                const __grid_constant__ CUtensorMap tmB, const TcParams p) {
     constexpr int CK = SWZ / 2;                     // BF16 elements per K chunk (one swizzle row)
@@ -257,21 +256,21 @@ uint32_t pow2_at_least(uint32_t v) {
     return c;
 }
 
-template <int MODE, int SWZ> size_t smem_bytes(int n_tile) {
+template <int MODE, int SWZ, int kStages> size_t smem_bytes(int n_tile) {
     const size_t a = 128u * SWZ, b = (((size_t)n_tile * SWZ) + 1023) & ~size_t(1023);
     return 1024 + kStages * (a + b) + 256;
 }
 
-template <int MODE, int SWZ> void launch_tc(dim3 grid, const CUtensorMap& a, const CUtensorMap& b, const TcParams& p,
-                                            cudaStream_t st) {
-    const size_t sm = smem_bytes<MODE, SWZ>(p.n_tile);
+template <int MODE, int SWZ, int kStages>
+void launch_tc(dim3 grid, const CUtensorMap& a, const CUtensorMap& b, const TcParams& p, cudaStream_t st) {
+    const size_t sm = smem_bytes<MODE, SWZ, kStages>(p.n_tile);
     static bool configured = false;
     if (!configured) {
-        KF_CUDA_CHECK(cudaFuncSetAttribute(k_tc<MODE, SWZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem_bytes<MODE, SWZ>(256)));
+        KF_CUDA_CHECK(cudaFuncSetAttribute(k_tc<MODE, SWZ, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem_bytes<MODE, SWZ, kStages>(256)));
         configured = true;
     }
-    k_tc<MODE, SWZ><<<grid, 128, sm, st>>>(a, b, p);
+    k_tc<MODE, SWZ, kStages><<<grid, 128, sm, st>>>(a, b, p);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -317,7 +316,12 @@ void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     p.out_coff = y_coff;
     p.tmem_cols = pow2_at_least((uint32_t)n_tile);
     const dim3 grid((unsigned)(p.tiles_x * p.tiles_y * N), (unsigned)((Cout_rows + n_tile - 1) / n_tile), 1);
-    launch_tc<0, 64>(grid, ma, mb, p, st);
+    // short K loops (Cin <= 64: 9 or 18 steps) take a 2-stage ring: half the shared memory,
+    // twice the resident CTAs, so one CTA's epilogue overlaps the others' loads and MMAs
+    if (p.k_iters <= 18)
+        launch_tc<0, 64, 2>(grid, ma, mb, p, st);
+    else
+        launch_tc<0, 64, 3>(grid, ma, mb, p, st);
 }
 
 void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, int K, float* d, int ldd, int splits,
@@ -347,7 +351,7 @@ void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, 
     p.tmem_cols = pow2_at_least((uint32_t)n_tile);
     const dim3 grid((unsigned)((M + 127) / 128), (unsigned)((N + n_tile - 1) / n_tile),
                     (unsigned)((p.k_iters + p.k_per_split - 1) / p.k_per_split));
-    launch_tc<1, 128>(grid, ma, mb, p, st);
+    launch_tc<1, 128, 4>(grid, ma, mb, p, st);
 }
 
 uint32_t tc_take_error() {

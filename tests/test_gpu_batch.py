@@ -33,11 +33,15 @@ def _check(r, scene, cam, cam_index, spp, depth, clear, use_bvh, env=False):
     return paths
 
 
-@pytest.mark.parametrize("traversal", [0, 1])
-def test_batch_of_uneven_views_matches_oracle(traversal):
+@pytest.mark.parametrize("traversal,chunk", [(0, 0), (1, 0), (1, 3000)])
+def test_batch_of_uneven_views_matches_oracle(traversal, chunk):
+    """chunk 3000: views split across chunks (camera rays queued per sample, or unpermuted
+    where a sample straddles two chunks)."""
     depth = 4
     cfg = scenes.cornell_config(spp=1, depth=depth, debug=True)
     cfg.setTraversal(traversal)
+    if chunk:
+        cfg._c.max_paths_in_flight = chunk
     with api.Kuafu(cfg) as r:
         s0 = r.getScene()
         c0 = scenes.cornell(r, 40, 32, scene=s0, variation=1)

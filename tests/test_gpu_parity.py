@@ -300,3 +300,21 @@ def test_graph_replay_matches_direct_launch():
             r.run()
             outs.append(r.downloadAov(cam, N.KF_AOV_RADIANCE_F32))
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_two_stream_schedule_matches_sequential():
+    """The default schedule runs each bounce's shadow traversal and gather on a second
+    stream beside the next bounce's closest-hit traversal; the profiling schedule runs every
+    kernel in order on one stream. Same bytes, with several chunks of paths."""
+    outs = []
+    for profile in (False, True):
+        cfg = scenes.icosphere_config(spp=3, depth=6, count=12)
+        cfg.setProfile(profile)
+        cfg._c.max_paths_in_flight = 4096  # several chunks, views split across them
+        with api.Kuafu(cfg) as r:
+            cam = scenes.icospheres(r, 64, 40, count=12, level=2)
+            r.run()
+            r.run()
+            outs.append((r.downloadAov(cam, N.KF_AOV_RADIANCE_F32), r.downloadLatestFrame(cam)))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
