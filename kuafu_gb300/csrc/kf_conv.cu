@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
     uint64_t* empty = full + kStages;
     uint64_t* done = empty + kStages;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    float* sbias = reinterpret_cast<float*>(tmem_slot + 4); // the tile's bias (0 where none)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -92,6 +93,9 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
     const int nk = max(0, k_end - k_begin);
 
     if (warp == 0) tc::tmem_alloc(tmem_slot, p.tmem_cols);
+    if (MODE == 0)
+        for (int i = threadIdx.x; i < p.n_tile; i += blockDim.x)
+            sbias[i] = (p.bias && n0 + i < p.Cout) ? p.bias[n0 + i] : 0.0f;
     if (threadIdx.x == 32) {
         for (int s = 0; s < kStages; ++s) {
             tc::mbar_init(&full[s], 1);
@@ -166,22 +170,20 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
         const int px = x0 + (row % p.bw), py = y0 + (row / p.bw);
         const bool valid = ready && nk > 0 && px < p.W && py < p.H;
         const size_t base = ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
-        for (int c = 0; c < p.n_tile; c += 8) {
-            uint32_t r[8];
-            tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
-            tc::tmem_ld_wait();
+        // 16 columns per TMEM wait: two loads in flight; bias from shared memory
+        auto emit8 = [&](const uint32_t(&r)[8], int c) {
             const int co = n0 + c;
-            if (!valid || co >= p.Cout) continue;
+            if (!valid || co >= p.Cout) return;
             float v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 v[j] = __uint_as_float(r[j]);
-                if (p.bias && co + j < p.Cout) v[j] += p.bias[co + j];
+                if (p.bias && co + j < p.Cout) v[j] += sbias[c + j];
                 if (p.relu) v[j] = fmaxf(v[j], 0.0f);
             }
             if (p.outf) { // FP32 output (a network head)
                 for (int j = 0; j < 8 && co + j < p.Cout; ++j) p.outf[base + co + j] = v[j];
-                continue;
+                return;
             }
             __nv_bfloat16* dst = p.out + base;
             if (co + 8 <= p.Cout && ((p.out_coff + co) & 7) == 0 && (p.out_cstride & 7) == 0) {
@@ -192,6 +194,14 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
             } else {
                 for (int j = 0; j < 8 && co + j < p.Cout; ++j) dst[co + j] = __float2bfloat16_rn(v[j]);
             }
+        };
+        for (int c = 0; c < p.n_tile; c += 16) {
+            uint32_t r0[8], r1[8];
+            tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r0);
+            tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c + 8), r1);
+            tc::tmem_ld_wait();
+            emit8(r0, c);
+            emit8(r1, c + 8);
         }
     } else {
         const int m = m0 + row;
@@ -258,7 +268,7 @@ uint32_t pow2_at_least(uint32_t v) {
 
 template <int MODE, int SWZ, int kStages> size_t smem_bytes(int n_tile) {
     const size_t a = 128u * SWZ, b = (((size_t)n_tile * SWZ) + 1023) & ~size_t(1023);
-    return 1024 + kStages * (a + b) + 256;
+    return 1024 + kStages * (a + b) + 256 + 4u * (size_t)n_tile;
 }
 
 template <int MODE, int SWZ, int kStages>
