@@ -897,15 +897,18 @@ __global__ void __launch_bounds__(kMissThreads) k_miss(SceneDev s, const FrameDe
     }
 }
 
+// Blocks of the shading kernels (k_shade, k_nee): their block scans keep one count per warp.
+constexpr uint32_t kShadeThreads = 128, kShadeWarps = kShadeThreads / 32;
+
 template <bool BATCH>
 // 4 resident blocks per SM (128 registers, no spill) measured fastest; unbounded it takes 148.
-__global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+__global__ void __launch_bounds__(kShadeThreads, 4) k_shade(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                                int cur, uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[5]; // rays of this bounce that hit (k_miss takes the others)
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ uint32_t s_cnt[2][4], s_base[2]; // per tile parity: the block scan of continuing paths
+    __shared__ uint32_t s_cnt[2][kShadeWarps], s_base[2]; // per tile parity: the block scan of continuing paths
     uint32_t par = 0;
     for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < count; bbase += stride, par ^= 1) {
         const uint32_t base = bbase + (threadIdx.x & ~31u);
@@ -1124,7 +1127,8 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
         if (lane == 0) s_cnt[par][wid] = __popc(m);
         __syncthreads();
         if (threadIdx.x == 0) {
-            const uint32_t t = s_cnt[par][0] + s_cnt[par][1] + s_cnt[par][2] + s_cnt[par][3];
+            uint32_t t = 0;
+            for (uint32_t k = 0; k < kShadeWarps; ++k) t += s_cnt[par][k];
             s_base[par] = t ? atomicAdd(&w.counters[nxt], t) : 0u;
         }
         __syncthreads();
@@ -1145,12 +1149,12 @@ __global__ void __launch_bounds__(128, 4) k_shade(SceneDev s, const FrameDev* __
 // small enough for the instruction cache.
 // ---------------------------------------------------------------------------
 template <bool BATCH>
-__global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
+__global__ void __launch_bounds__(kShadeThreads) k_nee(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                              uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[5];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ uint32_t s_cnt[2][4], s_base[2]; // per slot parity: the block scan of emitted rays
+    __shared__ uint32_t s_cnt[2][kShadeWarps], s_base[2]; // per slot parity: the block scan of emitted rays
     uint32_t par = 0;
     for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < count; bbase += stride) {
         const uint32_t base = bbase + (threadIdx.x & ~31u);
@@ -1206,7 +1210,8 @@ __global__ void __launch_bounds__(128) k_nee(SceneDev s, const FrameDev* __restr
                 if (lane == 0) s_cnt[par][wid] = __popc(m);
                 __syncthreads();
                 if (threadIdx.x == 0) {
-                    const uint32_t t = s_cnt[par][0] + s_cnt[par][1] + s_cnt[par][2] + s_cnt[par][3];
+                    uint32_t t = 0;
+            for (uint32_t k = 0; k < kShadeWarps; ++k) t += s_cnt[par][k];
                     s_base[par] = t ? atomicAdd(&w.scount[j], t) : 0u;
                 }
                 __syncthreads();
@@ -1524,9 +1529,9 @@ void launch_extend(const SceneDev& s, const FrameDev* f, const BatchDev& b, cons
 void launch_shade(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
                   uint32_t depth, uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
     if (b.items)
-        k_shade<true><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        k_shade<true><<<grid, kShadeThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     else
-        k_shade<false><<<grid, 128, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
+        k_shade<false><<<grid, kShadeThreads, 0, st>>>(s, f, b, w, cur, depth, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, int cur,
@@ -1540,9 +1545,9 @@ void launch_miss(const SceneDev& s, const FrameDev* f, const BatchDev& b, const 
 void launch_nee(const SceneDev& s, const FrameDev* f, const BatchDev& b, const WaveDev& w, uint32_t depth,
                 uint64_t chunk_start, uint32_t grid, cudaStream_t st) {
     if (b.items)
-        k_nee<true><<<grid, 128, 0, st>>>(s, f, b, w, depth, chunk_start);
+        k_nee<true><<<grid, kShadeThreads, 0, st>>>(s, f, b, w, depth, chunk_start);
     else
-        k_nee<false><<<grid, 128, 0, st>>>(s, f, b, w, depth, chunk_start);
+        k_nee<false><<<grid, kShadeThreads, 0, st>>>(s, f, b, w, depth, chunk_start);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 void launch_shadow(const SceneDev& s, const BatchDev& b, const WaveDev& w, uint32_t grid, bool count_mode,
