@@ -10,8 +10,8 @@
 //   * K-major GEMM D += A * B^T (weight gradients): 2D TMA, 128-byte swizzle,
 //     split-K with FP32 atomics in the epilogue.
 //
-// One CTA of 128 threads per output tile: warp 0 lane 0 issues TMA into a 4-stage
-// mbarrier ring, warp 1 lane 0 issues the MMAs, all four warps drain TMEM. Every
+// One CTA of 128 threads per output tile: warp 0 lane 0 issues TMA into a 2-, 3- or
+// 4-stage mbarrier ring, warp 1 lane 0 issues the MMAs, all four warps drain TMEM. Every
 // wait is bounded (~1 s of SM clock); on expiry the kernel records an error code,
 // drains its own copies and frees its TMEM.
 #include <cuda.h>
