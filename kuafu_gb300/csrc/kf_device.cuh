@@ -203,6 +203,8 @@ static_assert(sizeof(Node4) == 128, "Node4 must be 128 bytes");
 // 0..25, so that the traversal pushes the link as it is. Rebasing a leaf by a primitive
 // offset is a plain addition (the sum stays below 2^26).
 constexpr uint32_t kLeafChildTag = 0x40000000u, kLeafFirstMask = 0x03FFFFFFu;
+// A TLAS leaf of one instance links the instance itself: bit 31 set, instance index below.
+constexpr uint32_t kInstChildTag = 0x80000000u;
 __host__ __device__ __forceinline__ int leaf_child(int first, int count) {
     return (int)(kLeafChildTag | ((uint32_t)(count - 1) << 26) | (uint32_t)first);
 }

@@ -51,9 +51,10 @@ __global__ void k_tri_gather(const float4* __restrict__ verts, const uint32_t* _
     out[j] = t;
 }
 
-// Rebase a freshly built node array into a pool: inner children += node_base,
-// leaf children += leaf_base.
-__global__ void k_rebase(const Node4* __restrict__ in, uint32_t n, uint32_t node_base, uint32_t leaf_base, Node4* out) {
+// Rebase a freshly built node array into a pool: inner children += node_base, leaf
+// children += leaf_base, instance links (TLAS leaves of one instance) += inst_base.
+__global__ void k_rebase(const Node4* __restrict__ in, uint32_t n, uint32_t node_base, uint32_t leaf_base,
+                         uint32_t inst_base, Node4* out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Node4 o = in[i];
@@ -61,7 +62,7 @@ __global__ void k_rebase(const Node4* __restrict__ in, uint32_t n, uint32_t node
     const int k[4] = {o.cnt.x, o.cnt.y, o.cnt.z, o.cnt.w};
     for (int q = 0; q < 4; ++q) {
         if (k[q] == 0) c[q] += (int)node_base;
-        else if (k[q] > 0) c[q] += (int)leaf_base;
+        else if (k[q] > 0) c[q] += (int)(((uint32_t)c[q] & kInstChildTag) ? inst_base : leaf_base);
     }
     o.child = make_int4(c[0], c[1], c[2], c[3]);
     out[i] = o;
@@ -283,7 +284,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             }
             k_tri_gather<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, order.ptr, geom[gi].x,
                                                              geom[gi].y, ntri, G.tris.ptr + geom[gi].y);
-            k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y,
+            k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y, 0u,
                                                        G.blas_nodes.ptr + node_base);
             KF_CUDA_CHECK(cudaGetLastError());
             Node4 root;
@@ -419,7 +420,9 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
                     hz[c] = std::max(std::max(k.hiz.x, k.hiz.y), std::max(k.hiz.z, k.hiz.w));
                 } else {
                     for (int q = 0; q < cn[c]; ++q) {
-                        const uint32_t id = G.tlas_host_inst[leaf_first(ch[c]) + q];
+                        const uint32_t id = ((uint32_t)ch[c] & kInstChildTag)
+                                                ? ((uint32_t)ch[c] & ~kInstChildTag)
+                                                : G.tlas_host_inst[leaf_first(ch[c]) + q];
                         lx[c] = std::min(lx[c], wlo[id].x); ly[c] = std::min(ly[c], wlo[id].y);
                         lz[c] = std::min(lz[c], wlo[id].z); hx[c] = std::max(hx[c], whi[id].x);
                         hy[c] = std::max(hy[c], whi[id].y); hz[c] = std::max(hz[c], whi[id].z);
@@ -486,6 +489,15 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             KF_CUDA_CHECK(cudaMemcpyAsync(G.tlas_host_inst.data(), G.tlas_inst.ptr, sizeof(uint32_t) * nv,
                                           cudaMemcpyDeviceToHost, st));
             KF_CUDA_CHECK(cudaStreamSynchronize(st));
+            // a leaf of one instance links the instance itself (the traversal enters it without
+            // reading the leaf list)
+            for (Node4& nd : G.tlas_host_nodes) {
+                int* ch = &nd.child.x;
+                const int* cn = &nd.cnt.x;
+                for (int c = 0; c < 4; ++c)
+                    if (cn[c] == 1) ch[c] = (int)(kInstChildTag | G.tlas_host_inst[leaf_first(ch[c])]);
+            }
+            G.tlas_nodes.upload(G.tlas_host_nodes.data(), G.tlas_host_nodes.size(), st);
         } else {
             G.tlas_node_count = 0;
             G.tlas_nodes.resize(1, st);
@@ -642,14 +654,14 @@ void batch_sync(kf_renderer_s* r, const std::vector<kf_scene_s*>& scenes) {
         }
         if (G.blas_node_count) {
             k_rebase<<<(G.blas_node_count + 127) / 128, 128, 0, st>>>(G.blas_nodes.ptr, G.blas_node_count,
-                                                                      (uint32_t)obn, (uint32_t)ot,
+                                                                      (uint32_t)obn, (uint32_t)ot, 0u,
                                                                       B.blas_nodes.ptr + obn);
             KF_CUDA_CHECK(cudaGetLastError());
         }
         if (G.tlas_node_count) {
             k_rebase<<<(G.tlas_node_count + 127) / 128, 128, 0, st>>>(G.tlas_nodes.ptr, G.tlas_node_count,
                                                                       (uint32_t)otn, (uint32_t)oti,
-                                                                      B.tlas_nodes.ptr + otn);
+                                                                      (uint32_t)oinst, B.tlas_nodes.ptr + otn);
             KF_CUDA_CHECK(cudaGetLastError());
             std::vector<uint32_t> ti(G.tlas_inst.count);
             KF_CUDA_CHECK(cudaMemcpyAsync(ti.data(), G.tlas_inst.ptr, ti.size() * 4, cudaMemcpyDeviceToHost, st));

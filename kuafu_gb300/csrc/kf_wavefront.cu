@@ -31,6 +31,7 @@ constexpr uint32_t kInstTag = 0x80000000u;
 constexpr uint32_t kPopTag = 0xC0000000u;
 constexpr uint32_t kLeafTag = 0x40000000u;
 static_assert(kLeafTag == kLeafChildTag, "leaf child links are pushed as stack entries");
+static_assert(kInstTag == kInstChildTag, "instance links of the TLAS are pushed as stack entries");
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 struct HitOut {
