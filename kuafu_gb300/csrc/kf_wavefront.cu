@@ -3,14 +3,17 @@
 // (resources/shaders/PathTrace.{rgen,rchit,rahit,rmiss}, PathTraceShadow.rmiss).
 //
 // One frame = every (pixel, sample) path of a camera, processed bounce by bounce:
-//   raygen   camera rays                                  (PathTrace.rgen:30-75)
+//   raygen   camera rays, queued in pixel tiles            (PathTrace.rgen:30-75)
 //   extend   closest hit, two-level BVH4 traversal         (traceRayEXT, rgen:97-107)
-//   shade    miss / emission / PrincipledBSDF sampling,    (PathTrace.rmiss, rchit:322-468)
-//            light samples -> shadow queue, RR             (rchit:204-316, rgen:109-138)
-//   shadow   any-hit occlusion of the shadow queue         (rchit:175-200)
+//   miss     environment / clear colour; lists the hits    (PathTrace.rmiss)
+//   shade    emission / PrincipledBSDF sampling, RR,       (rchit:322-468, rgen:109-138)
+//            next ray, NEE record
+//   nee      light samples -> one shadow queue per light   (rchit:204-316)
+//   shadow   any-hit occlusion of the shadow queues        (rchit:175-200)
 //   gather   ordered NEE sum into the path radiance        (rchit:457-460, rgen:111)
 // then a per-pixel resolve (rgen:140-166) and the sRGB frame (PostProcessing.frag).
-// Queues are compacted with warp ballots + one atomic per warp.
+// Queues are compacted in order: a block scan per tile with one atomic per tile (warp
+// ballots + one atomic per warp where the warps of a block differ).
 //
 // This file is compiled with -fmad=false: float expressions round exactly as
 // written, matching the CPU oracle operation for operation.
@@ -165,7 +168,8 @@ template <bool SHADOW, bool COUNT> struct Tracer {
 
     // Returns true when the traversal is over (stack empty, or the first hit of a shadow ray).
     // Stack entries: kPopTag (back to the TLAS), kInstTag | instance, kLeafTag | (n-1) << 26 |
-    // first triangle (a BLAS leaf of n triangles), or a node index.
+    // first (a BLAS leaf of n triangles, or a TLAS leaf of n instances in the leaf list), or a
+    // node index. Node child links are entries of these kinds as they are.
     // The rare, cheap entries do not take a step of their own: a return to the TLAS goes on
     // to the next entry (a TLAS node or instance), and an instance entry goes on to the root
     // node of its BLAS, so the lanes of a warp mostly run the node or the leaf code together.
