@@ -374,7 +374,8 @@ KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* 
                                   int h, int w, float lr, float* grads_dev, int apply, float* loss);
 
 /* ---- FP64 relative-MSE reduction: mean over pixels and channels of
- * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64 ---- */
+ * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64;
+ * num_pixels > 0 ---- */
 KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
                      double* out);
 
@@ -383,9 +384,10 @@ KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, ui
  * must not take the device-wide synchronisation cudaMalloc / cudaFree imply.
  * It allocates nothing: its per-block partials live in a static device array of
  * 4096 + 1 doubles (32 KiB) that every GPU loading libkf keeps until exit.
- * Limit: num_pixels <= 268435456 (4096 blocks x 65536 pixels), else KF_ERR_LIMIT.
- * Runs on `stream` (a cudaStream_t, NULL = default stream) of the current device;
- * the first call on a device looks up the array's device address, so make that
+ * Limit: 0 < num_pixels <= 268435456 (2^28), else KF_ERR_INVALID_ARGUMENT /
+ * KF_ERR_LIMIT. Runs on `stream` (a cudaStream_t, NULL = default stream) of the
+ * current device. Every call looks up the array's device address on the current
+ * device; the first call on a device also loads the module there, so make that
  * first call before any stream capture. Calls share the array: calls that overlap
  * on the GPU (other streams, other threads) race and must be serialised by the
  * caller. Blocks until *out is written. No counterpart in the reference. */

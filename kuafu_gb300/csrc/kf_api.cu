@@ -1233,6 +1233,7 @@ KF_API int kf_camera_get_ubo(kf_camera c, kf_camera_ubo* out) {
 KF_API int kf_relmse(kf_renderer r, const float* x, const float* ref, uint64_t n, double eps, double* out) {
     return guarded([&] {
         REQ(r && x && ref && out, "null argument");
+        REQ(n > 0, "relMSE over zero pixels");
         require_device(r);
         const uint32_t blocks = (uint32_t)std::max(1, std::min(r->num_sms * 4, (int)((n + 255) / 256)));
         if (r->scratch64.count < (size_t)blocks + 1) r->scratch64.resize(blocks + 1, r->stream);

@@ -385,6 +385,30 @@ static std::string launch_shape_key(const kf_renderer_s* r) {
     return b;
 }
 
+// Everything of a scene's device view that a captured graph bakes into its kernel
+// parameters (SceneDev is passed by value): buffer addresses, counts and the light-slot
+// map. The slot map is rebuilt every frame from the light UBOs without moving a buffer,
+// so switching which lights are on at an unchanged count must still recapture.
+static std::string scene_view_key(const SceneDev& v) {
+    std::string k;
+    char b[64];
+    const void* ptrs[] = {v.verts, v.indices, v.matidx, v.geom, v.materials, v.inst, v.blas_nodes, v.tris,
+                          v.tlas_nodes, v.tlas_inst, v.dlight, v.plights, v.alights, v.tex_info, v.texels,
+                          v.srgb_decode, v.env};
+    for (const void* p : ptrs) {
+        std::snprintf(b, sizeof(b), "%p,", p);
+        k += b;
+    }
+    std::snprintf(b, sizeof(b), "%u,%u,%u,%u,%u:", v.env_size, v.num_instances, v.has_tlas, v.num_textures,
+                  v.num_slots);
+    k += b;
+    for (uint32_t j = 0; j < v.num_slots && j < (uint32_t)kMaxLightSlots; ++j) {
+        std::snprintf(b, sizeof(b), "%u.%u,", (unsigned)v.slot_group[j], (unsigned)v.slot_index[j]);
+        k += b;
+    }
+    return k;
+}
+
 static uint32_t chunk_for(const kf_renderer_s* r, uint64_t npaths) {
     uint64_t cap = r->cfg.max_paths_in_flight ? r->cfg.max_paths_in_flight : (1ull << 24);
     cap = std::min<uint64_t>(cap, (1ull << 26) - 1);
@@ -422,12 +446,13 @@ void render_frame(kf_renderer_s* r, kf_scene_s* s, kf_camera_s* c, uint32_t spp)
     if (use_graph) {
         // The launch sequence depends only on buffer addresses and sizes; the
         // per-frame values live in frame_dev, so a captured graph replays as is.
-        char key[512];
-        std::snprintf(key, sizeof(key), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%u|%s", (void*)s, (void*)c,
+        char head[512];
+        std::snprintf(head, sizeof(head), "%p|%p|%llu|%u|%u|%u|%llu|%u|%p|%p|%p|%p|%p|%u|%s|", (void*)s, (void*)c,
                       (unsigned long long)s->gpu.generation, npix, spp, r->cfg.path_depth,
                       (unsigned long long)npaths, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)w.contrib,
-                      (void*)c->accum.ptr, (void*)w.primary, sv.num_slots,
-                      r->cfg.russian_roulette | (r->cfg.traversal << 1), launch_shape_key(r).c_str());
+                      (void*)c->accum.ptr, (void*)w.primary, r->cfg.russian_roulette | (r->cfg.traversal << 1),
+                      launch_shape_key(r).c_str());
+        const std::string key = std::string(head) + scene_view_key(sv);
         if (!r->graph_exec || r->graph_key != key) {
             if (r->graph_exec) {
                 cudaGraphExecDestroy(r->graph_exec);
@@ -554,7 +579,7 @@ void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count) 
         std::snprintf(buf, sizeof(buf), "%llu|%u|%llu|%u|%p|%p|%p|%u|%u|", (unsigned long long)B.generation, count,
                       (unsigned long long)total, chunk, (void*)w.q_o[0], (void*)w.radiance, (void*)B.items.ptr,
                       r->cfg.path_depth, r->cfg.russian_roulette | (r->cfg.traversal << 1));
-        key = buf + launch_shape_key(r) + "|";
+        key = buf + launch_shape_key(r) + "|" + scene_view_key(B.view) + "|";
         for (uint32_t i = 0; i < count; ++i) {
             std::snprintf(buf, sizeof(buf), "%p,%u,%u;", (void*)items[i].camera->accum.ptr, hv[i].f.npix,
                           items[i].spp);

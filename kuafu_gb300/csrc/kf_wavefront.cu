@@ -19,7 +19,6 @@
 // written, matching the CPU oracle operation for operation.
 #include "kf_wavefront.h"
 
-#include <mutex>
 #include <string>
 
 #include "kf_util.h"
@@ -1647,11 +1646,8 @@ void launch_relmse(const float4* x, const float4* ref, uint64_t n, double eps, d
 // ---------------------------------------------------------------------------
 namespace {
 constexpr uint32_t kNoAllocMaxBlocks = 4096;
-constexpr uint64_t kNoAllocPixelsPerBlock = 65536;
+constexpr uint64_t kNoAllocMaxPixels = 268435456ull; // 2^28: the stated per-call limit
 static __device__ __align__(256) double g_relmse_scratch[kNoAllocMaxBlocks + 1];
-
-std::mutex g_noalloc_mu;
-double* g_noalloc_addr[256] = {}; // device address of g_relmse_scratch, per device ordinal
 } // namespace
 
 namespace kf {
@@ -1664,34 +1660,32 @@ extern "C" KF_API int kf_relmse_noalloc(const float* x_dev, const float* ref_dev
         kf::set_last_error("kf_relmse_noalloc: null pointer or zero pixels");
         return KF_ERR_INVALID_ARGUMENT;
     }
-    if (num_pixels > (uint64_t)kNoAllocMaxBlocks * kNoAllocPixelsPerBlock) {
-        kf::set_last_error("kf_relmse_noalloc: more than 268435456 pixels (4096 blocks x 65536 pixels) do not fit "
-                           "its static scratch; use kf_relmse");
+    if (num_pixels > kNoAllocMaxPixels) {
+        kf::set_last_error("kf_relmse_noalloc: more than 268435456 pixels per call exceed the limit of its static "
+                           "scratch; use kf_relmse");
         return KF_ERR_LIMIT;
     }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
         kf::set_last_error("kf_relmse_noalloc: no current CUDA device");
         return KF_ERR_NO_DEVICE;
     }
-    double* scratch = nullptr;
-    {
-        // set-up, once per device with that device current: the host-side name of the
-        // array is not a device address, so ask the runtime for the device address.
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
-            void* p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_relmse_scratch);
-            if (e != cudaSuccess || !p) {
-                kf::set_last_error(std::string("kf_relmse_noalloc: cudaGetSymbolAddress failed: ") +
-                                   cudaGetErrorString(e));
-                return KF_ERR_CUDA;
-            }
-            g_noalloc_addr[dev] = static_cast<double*>(p);
-        }
-        scratch = g_noalloc_addr[dev];
+    // The host-side name of the array is not a device address: ask the runtime for the
+    // address on the current device, on every call (it is cheap beside the launches and
+    // the synchronisation, and stays right if the device's context was re-created). The
+    // first call on a device loads the module there.
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_relmse_scratch);
+    if (e != cudaSuccess || !p) {
+        kf::set_last_error(std::string("kf_relmse_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        return KF_ERR_CUDA;
     }
-    const uint32_t blocks = (uint32_t)((num_pixels + kNoAllocPixelsPerBlock - 1) / kNoAllocPixelsPerBlock);
+    double* scratch = static_cast<double*>(p);
+    // k_relmse_partial is a grid-stride loop: 4 blocks per SM fill the GPU, at most one
+    // block per 256 pixels, and never more blocks than the array holds partials
+    const uint64_t want = std::min<uint64_t>((num_pixels + 255) / 256, (uint64_t)sms * 4);
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, kNoAllocMaxBlocks));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // every partial in [0, blocks) and the result slot are written before they are read,
     // so nothing needs clearing between calls
@@ -1699,7 +1693,7 @@ extern "C" KF_API int kf_relmse_noalloc(const float* x_dev, const float* ref_dev
                                                   reinterpret_cast<const float4*>(ref_dev), num_pixels, eps,
                                                   scratch);
     kf::k_relmse_final<<<1, 256, 0, st>>>(scratch, blocks, num_pixels, scratch + kNoAllocMaxBlocks);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, scratch + kNoAllocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -206,3 +206,17 @@ def test_cornell_export_shape():
         w2o = np.array(inst.world_to_object[:], np.float64).reshape(3, 4)
         prod = w2o @ m
         assert np.allclose(prod[:, :3], np.eye(3), atol=1e-5)
+
+
+def test_relmse_entry_points_reject_zero_pixels():
+    """kf_relmse and kf_relmse_noalloc agree: a mean over zero pixels is an invalid
+    argument, refused before anything touches a device."""
+    import ctypes as C
+
+    lib = N.load()
+    got = C.c_double()
+    assert lib.kf_relmse_noalloc(C.c_void_p(16), C.c_void_p(16), 0, 1e-2, None, C.byref(got)) == 1
+    r = host_renderer()
+    assert lib.kf_relmse(r._h, C.c_void_p(16), C.c_void_p(16), 0, 1e-2, C.byref(got)) == 1
+    assert b"zero pixels" in lib.kf_last_error()
+    r.close()

@@ -1,0 +1,203 @@
+"""Parity at the benchmark configurations themselves, not only at small stand-ins.
+
+* Cornell box, 256x256, 64 spp, path depth 5, Russian roulette off (kuafu's example
+  settings, example/main.cpp:20): every path of the full frame against the oracle.
+* 256 level-4 icospheres (1.31 M triangles), 1920x1080, 8 spp, depth 8, Russian roulette
+  from bounce 4, 1 directional + 4 point + 2 spot lights, background 0.1 (the Mrays/s
+  workload): the GPU renders the whole frame, the oracle traverses its own CPU BVH for
+  fixed crops of it (deep BLAS, long traversal stacks, 9-trace paths).
+* Both BVH builders (GPU LBVH and host binned SAH) give the same hits and paths.
+* Converged FP64 accumulation: the GPU's FP64 sum of 1024 spp against the oracle's FP64
+  render, on the same sample streams (agreement far below the noise) and on independent
+  streams (agreement within the noise floor of 1024 spp).
+
+Bar: primary-hit instance / primitive ids and hit distances bit-exact, per-path radiance
+within 1e-4 relative (FP32) for at least 99.9 % of the paths.
+"""
+import numpy as np
+import pytest
+
+from kuafu_gb300 import _native as N
+from kuafu_gb300 import api, scenes
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-4  # per-path radiance, FP32
+MIN_WITHIN = 0.999
+
+
+def _within(gpu_paths, ref_paths):
+    g = gpu_paths[..., :3].astype(np.float64)
+    c = ref_paths.astype(np.float64)
+    per_path = (np.abs(g - c) / np.maximum(np.abs(c), 1e-6)).max(axis=-1)
+    return (per_path <= REL_TOL).mean(), (gpu_paths[..., :3] == ref_paths).all(axis=-1).mean()
+
+
+def _relmse(x, ref, eps=1e-2):
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(((x - ref) ** 2 / (ref ** 2 + eps)).mean())
+
+
+def test_cornell_full_config_256x256_64spp_depth5():
+    spp, depth, w, h = 64, 5, 256, 256
+    cfg = scenes.cornell_config(spp=spp, depth=depth, debug=True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, w, h)
+        r.run()
+        paths = r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp)
+        hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)
+        rgba = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
+        flat = r.getScene().export()
+        ref = O.render(flat, cam.ubo(), w, h, O.push_constants(spp, depth), seed=0, frame=0, camera_index=1)
+    rh = ref["hits"]
+    assert np.array_equal(hits["instance"], rh["instance"])
+    hit = rh["instance"] != 0xFFFFFFFF
+    assert hit.mean() > 0.9  # a square 40 degree view sees the inside of the box
+    assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
+    assert np.array_equal(hits["t"][hit], rh["t"][hit])
+    within, exact = _within(paths, ref["paths"])
+    print(f"C1 full: {paths.shape[0] * w * h} paths, within 1e-4 {within:.6f}, bit-exact {exact:.6f}")
+    assert within >= MIN_WITHIN
+    assert np.allclose(rgba[..., :3], ref["pixel"], rtol=1e-5, atol=1e-6)
+
+
+# Crops of the 1920x1080 frame: mostly spheres, a sparse region and the frame centre.
+C2_CROPS = [(1200, 700, 96, 96), (600, 300, 96, 96), (912, 492, 96, 96)]
+
+
+@pytest.fixture(scope="module")
+def c2_frame():
+    spp, depth, w, h = 8, 8, 1920, 1080
+    cfg = scenes.icosphere_config(spp=spp, depth=depth, count=256)
+    cfg.setDebugOutputs(True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.icospheres(r, w, h, count=256, level=4, seed=0)
+        r.run()
+        st = r.stats()
+        out = {
+            "paths": r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp),
+            "hits": r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp),
+            "flat_ubo": (r.getScene().export(), cam.ubo()),
+            "rays": (st.rays_primary, st.rays_extension, st.rays_shadow),
+        }
+        yield out
+
+
+@pytest.mark.parametrize("crop", C2_CROPS)
+def test_icospheres_full_scene_1080p_crop(c2_frame, crop):
+    spp, depth = 8, 8
+    flat, ubo = c2_frame["flat_ubo"]
+    pc = O.push_constants(spp, depth, clear=(0.1, 0.1, 0.1, 1.0), rr=True, rr_min=4)
+    ref = O.render(flat, ubo, 1920, 1080, pc, seed=0, frame=0, camera_index=1, use_bvh=True, crop=crop)
+    x0, y0, cw, ch = crop
+    hits = c2_frame["hits"][:, y0:y0 + ch, x0:x0 + cw]
+    paths = c2_frame["paths"][:, y0:y0 + ch, x0:x0 + cw]
+    rh = ref["hits"]
+    assert np.array_equal(hits["instance"], rh["instance"])
+    hit = rh["instance"] != 0xFFFFFFFF
+    assert hit.any()
+    assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
+    assert np.array_equal(hits["t"][hit], rh["t"][hit])
+    assert np.array_equal(hits["u"][hit], rh["u"][hit]) and np.array_equal(hits["v"][hit], rh["v"][hit])
+    within, exact = _within(paths, ref["paths"])
+    print(f"C2 crop {crop}: hit {hit.mean():.3f}, deepest path {ref['depths'].max()} traces, "
+          f"within 1e-4 {within:.6f}, bit-exact {exact:.6f}")
+    assert within >= MIN_WITHIN
+
+
+def test_icospheres_full_scene_ray_count(c2_frame):
+    """All 16.6 M camera rays are traced; the frame issues extension and shadow rays."""
+    prim, ext, shadow = c2_frame["rays"]
+    assert prim == 1920 * 1080 * 8
+    assert ext > 0.3 * prim and shadow > prim
+
+
+@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("leaf", [1, 4, 16])
+def test_both_bvh_builders_find_the_same_hits(builder, leaf):
+    """GPU LBVH (bvh_builder 0) and host binned SAH (1) change the tree, never the hits."""
+    spp, depth = 2, 3
+    cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
+    cfg.setDebugOutputs(True)
+    cfg.setBvhBuilder(builder)
+    cfg.setBlasLeafSize(leaf)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.icospheres(r, 80, 48, count=24, level=2)
+        r.run()
+        paths = r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp)
+        hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)
+        st = r.stats()
+        assert st.blas_nodes > 0
+        ref = O.render(r.getScene().export(), cam.ubo(), 80, 48,
+                       O.push_constants(spp, depth, clear=(0.1, 0.1, 0.1, 1.0)), seed=0, frame=0, camera_index=1,
+                       use_bvh=True)
+    rh = ref["hits"]
+    assert np.array_equal(hits["instance"], rh["instance"])
+    hit = rh["instance"] != 0xFFFFFFFF
+    assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
+    assert np.array_equal(hits["t"][hit], rh["t"][hit])
+    within, _ = _within(paths, ref["paths"])
+    assert within >= MIN_WITHIN
+
+
+def test_gpu_lbvh_on_the_full_icosphere_scene():
+    """The GPU LBVH builds the 256 BLAS of the 1.31 M-triangle scene; its hits equal the
+    host SAH tree's over the whole 1080p frame."""
+    res = []
+    for builder in (0, 1):
+        cfg = scenes.icosphere_config(spp=1, depth=1, count=256)
+        cfg.setDebugOutputs(True)
+        cfg.setBvhBuilder(builder)
+        with api.Kuafu(cfg) as r:
+            cam = scenes.icospheres(r, 1920, 1080, count=256, level=4, seed=0)
+            r.run()
+            res.append(r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, 1))
+    assert np.array_equal(res[0]["instance"], res[1]["instance"])
+    hit = res[0]["instance"] != 0xFFFFFFFF
+    assert hit.mean() > 0.2
+    assert np.array_equal(res[0]["prim"][hit], res[1]["prim"][hit])
+    assert np.array_equal(res[0]["t"][hit], res[1]["t"][hit])
+
+
+def test_converged_fp64_accumulation_against_fp64_oracle():
+    """The FP64 sum target (KF_AOV_SUM_F64) over 64 frames x 16 spp = 1024 spp of a 48x48
+    Cornell view against the oracle's FP64 render of the same frames. Same sample streams:
+    the images differ only by FP32-vs-FP64 rounding (relMSE far below the 1024-spp noise).
+    Independent streams (seed 1): relMSE within twice the expected noise of two
+    independent 1024-spp estimates, measured from the oracle's own half-split."""
+    frames, spp, depth, w, h = 64, 16, 5, 48, 48
+    cfg = scenes.cornell_config(spp=spp, depth=depth)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, w, h)
+        for _ in range(frames):
+            r.run()
+        s64 = r.downloadAov(cam, N.KF_AOV_SUM_F64)
+        flat = r.getScene().export()
+        ubo = cam.ubo()
+    assert s64.dtype == np.float64 and (s64[..., 3] == frames).all()
+    gpu = s64[..., :3] / frames
+
+    def oracle_frames(seed):
+        acc = []
+        for f in range(frames):
+            res = O.render(flat, ubo, w, h, O.push_constants(spp, depth), seed=seed, frame=f, camera_index=1,
+                           precision=O.FP64, want_paths=False, want_hits=False)
+            acc.append(res["pixel64"])
+        return np.stack(acc)
+
+    same = oracle_frames(0)
+    indep = oracle_frames(1)
+    ref_same = same.mean(axis=0)
+    ref_indep = indep.mean(axis=0)
+    # noise of a 1024-spp estimate: relMSE(A, B) of two 512-spp halves is 4x it
+    half = _relmse(indep[: frames // 2].mean(axis=0), indep[frames // 2:].mean(axis=0))
+    floor_1024 = half / 4.0
+    r_same = _relmse(gpu, ref_same)
+    r_indep = _relmse(gpu, ref_indep)
+    print(f"FP64 converged: relMSE same streams {r_same:.3e}, independent {r_indep:.3e}, "
+          f"1024-spp floor {floor_1024:.3e}")
+    assert floor_1024 > 0
+    assert r_same < 1e-3 * floor_1024
+    assert r_indep < 2.0 * (2.0 * floor_1024)

@@ -154,25 +154,6 @@ def test_icospheres_with_lights_bvh_parity(traversal):
         assert st.rays_primary == 96 * 64 * spp
 
 
-@pytest.mark.parametrize("leaf", [1, 4, 16])
-def test_sah_built_bvh_finds_the_same_hits(leaf):
-    """The host binned-SAH builder (bvh_builder = 1) changes the tree, never the hits."""
-    spp, depth = 2, 3
-    cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
-    cfg.setDebugOutputs(True)
-    cfg.setBvhBuilder(1)
-    cfg.setBlasLeafSize(leaf)
-    with api.Kuafu(cfg) as r:
-        cam = scenes.icospheres(r, 80, 48, count=24, level=2)
-        paths, hits, rgba, ref = _render_pair(r, cam, spp, depth, clear=(0.1, 0.1, 0.1, 1.0), use_bvh=True)
-        rh = ref["hits"]
-        assert np.array_equal(hits["instance"], rh["instance"])
-        hit = rh["instance"] != 0xFFFFFFFF
-        assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
-        assert np.array_equal(hits["t"][hit], rh["t"][hit])
-        _check_paths(paths, ref["paths"])
-
-
 def test_loaded_obj_renders_like_the_oracle(tmp_path):
     """A quad-faced OBJ box without normals (fan triangulation, flat normals, MTL material
     with Ns -> roughness) loaded by kf_load_scene, inside the Cornell box."""
