@@ -316,6 +316,13 @@ typedef struct kf_autotune_result {
 KF_API int kf_renderer_autotune(kf_renderer r, const kf_batch_item* items, uint32_t count, uint32_t reps,
                                 kf_autotune_result* out);
 
+/* Achievable L2 read bandwidth of the renderer's GPU in GB/s: a `bytes` buffer (1 MiB ..
+ * 1 GiB; one that fits in L2, e.g. 32 MiB) read `passes` times through L2 by a
+ * full-occupancy grid, best of `reps` CUDA-event-timed launches on the renderer's stream.
+ * The denominator of the traversal kernels' L2 roofline. No counterpart in kuafu. */
+KF_API int kf_renderer_measure_l2_read(kf_renderer r, uint64_t bytes, uint32_t passes, uint32_t reps,
+                                       double* gbs);
+
 /* ---- tensor-core building blocks of the learned denoiser (device pointers; no
  * counterpart in kuafu, whose OptiX denoiser is closed code, denoiser.cpp:257-316) ---- */
 /* y[n,y,x,y_coff+co] = act(bias[co] + sum x[n,y+dy,x+dx,ci] * w[tap][co][ci]), NHWC BF16,

@@ -230,6 +230,7 @@ PROTOTYPES = {
     "kf_renderer_autotune": (I, [VP, C.POINTER(kf_batch_item), U32, U32, C.POINTER(kf_autotune_result)]),
     "kf_relmse": (I, [VP, VP, VP, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
     "kf_relmse_noalloc": (I, [VP, VP, C.c_uint64, C.c_double, VP, C.POINTER(C.c_double)]),
+    "kf_renderer_measure_l2_read": (I, [VP, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]),
     "kf_conv3x3_bf16": (I, [VP, I, I, I, I, VP, I, VP, I, I, VP, I, I, VP]),
     "kf_gemm_bf16_tn": (I, [VP, I, VP, I, I, VP, I, I, VP]),
     "kf_tc_error": (I, [C.POINTER(U32)]),

@@ -477,6 +477,12 @@ class Kuafu:
     def run(self):
         N.check(_lib().kf_renderer_run(self._h))
 
+    def measureL2Read(self, bytes=32 << 20, passes=64, reps=5) -> float:
+        """Achievable L2 read bandwidth of this renderer's GPU, GB/s (kf_renderer_measure_l2_read)."""
+        out = C.c_double()
+        N.check(_lib().kf_renderer_measure_l2_read(self._h, int(bytes), int(passes), int(reps), C.byref(out)))
+        return out.value
+
     def synchronize(self):
         N.check(_lib().kf_renderer_synchronize(self._h))
 

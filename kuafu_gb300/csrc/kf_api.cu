@@ -394,6 +394,16 @@ KF_API int kf_renderer_autotune(kf_renderer r, const kf_batch_item* items, uint3
     });
 }
 
+KF_API int kf_renderer_measure_l2_read(kf_renderer r, uint64_t bytes, uint32_t passes, uint32_t reps,
+                                       double* gbs) {
+    return guarded([&] {
+        REQ(r && gbs, "null argument");
+        REQ(bytes >= (1u << 20) && bytes <= (1ull << 30), "probe size must be in [1 MiB, 1 GiB]");
+        require_device(r);
+        *gbs = measure_l2_read(r, bytes, passes, reps);
+    });
+}
+
 KF_API int kf_renderer_synchronize(kf_renderer r) {
     return guarded([&] {
         REQ(r, "invalid renderer");

@@ -5,6 +5,9 @@
 // shape), one knob at a time (coordinate descent), each candidate timed with CUDA events
 // on the renderer's stream over `reps` batches after one warm-up batch (which also
 // captures the batch graph and, for a new leaf size, rebuilds every BLAS).
+//
+// It also holds the L2 read-bandwidth probe that the traversal's roofline is stated
+// against: the achievable rate at which this GPU's SMs read data that sits in L2.
 #include <algorithm>
 #include <vector>
 
@@ -149,6 +152,69 @@ void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count
         out->start_blas_leaf_size = start.leaf;
         out->start_max_paths_in_flight = start.chunk;
     }
+}
+
+// ---------------------------------------------------------------------------
+// L2 read bandwidth. A buffer that fits in L2 (the caller's size, 32 MiB by default
+// against the 126 MB L2) is read `passes` times by a full-occupancy grid with
+// ld.global.cg (cached in L2 only, so L1 does not serve repeats); every thread keeps
+// four independent 16-byte loads in flight per iteration. One untimed pass brings the
+// buffer into L2; the timed launch is bracketed by CUDA events on the renderer's
+// stream. Rate = passes x bytes / time, the best of `reps` launches.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kL2Threads = 512;
+
+__global__ void __launch_bounds__(kL2Threads) k_l2_read(const float4* __restrict__ buf, uint64_t n4, uint32_t passes,
+                                                         uint32_t* sink) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t acc = 0;
+    for (uint32_t p = 0; p < passes; ++p) {
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 3 * stride < n4; i += 4 * stride) {
+            const float4 a = __ldcg(buf + i);
+            const float4 b = __ldcg(buf + i + stride);
+            const float4 c = __ldcg(buf + i + 2 * stride);
+            const float4 d = __ldcg(buf + i + 3 * stride);
+            acc ^= __float_as_uint(a.x) ^ __float_as_uint(a.y) ^ __float_as_uint(a.z) ^ __float_as_uint(a.w);
+            acc ^= __float_as_uint(b.x) ^ __float_as_uint(b.y) ^ __float_as_uint(b.z) ^ __float_as_uint(b.w);
+            acc ^= __float_as_uint(c.x) ^ __float_as_uint(c.y) ^ __float_as_uint(c.z) ^ __float_as_uint(c.w);
+            acc ^= __float_as_uint(d.x) ^ __float_as_uint(d.y) ^ __float_as_uint(d.z) ^ __float_as_uint(d.w);
+        }
+    }
+    if (acc == 0x9E3779B9u) sink[0] = acc; // keeps the loads; practically never taken
+}
+} // namespace
+
+double measure_l2_read(kf_renderer_s* r, uint64_t bytes, uint32_t passes, uint32_t reps) {
+    int dev = 0;
+    KF_CUDA_CHECK(cudaGetDevice(&dev));
+    int per_sm = 0;
+    KF_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_l2_read, kL2Threads, 0));
+    const uint32_t grid = (uint32_t)std::max(1, r->num_sms) * (uint32_t)std::max(1, per_sm);
+    const uint64_t chunk = 4ull * grid * kL2Threads; // float4 per iteration of the whole grid
+    const uint64_t n4 = std::max<uint64_t>(1, bytes / 16 / chunk) * chunk;
+    passes = std::max(1u, passes);
+    reps = std::max(1u, reps);
+    cudaStream_t st = r->stream;
+    TempAlloc tmp(st);
+    float4* buf = tmp.alloc<float4>(n4);
+    uint32_t* sink = tmp.alloc<uint32_t>(1);
+    KF_CUDA_CHECK(cudaMemsetAsync(buf, 0x3C, n4 * sizeof(float4), st));
+    k_l2_read<<<grid, kL2Threads, 0, st>>>(buf, n4, 1, sink); // into L2
+    KF_CUDA_CHECK(cudaGetLastError());
+    cudaEvent_t e0 = r->ev[6], e1 = r->ev[7];
+    float best = 0.0f;
+    for (uint32_t i = 0; i < reps; ++i) {
+        KF_CUDA_CHECK(cudaEventRecord(e0, st));
+        k_l2_read<<<grid, kL2Threads, 0, st>>>(buf, n4, passes, sink);
+        KF_CUDA_CHECK(cudaEventRecord(e1, st));
+        KF_CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        if (i == 0 || ms < best) best = ms;
+    }
+    KF_CUDA_CHECK(cudaGetLastError());
+    return (double)n4 * 16.0 * passes / (best * 1e-3) / 1e9;
 }
 
 } // namespace kf

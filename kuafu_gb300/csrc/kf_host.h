@@ -232,6 +232,8 @@ void render_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count);
 // kf_renderer_autotune (kf_autotune.cu)
 void autotune_batch(kf_renderer_s* r, const kf_batch_item* items, uint32_t count, uint32_t reps,
                     kf_autotune_result* out);
+// Achievable L2 read bandwidth in GB/s (kf_autotune.cu).
+double measure_l2_read(kf_renderer_s* r, uint64_t bytes, uint32_t passes, uint32_t reps);
 
 // global tables
 std::vector<kf_material_gpu> flatten_materials();

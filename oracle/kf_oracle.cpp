@@ -25,10 +25,12 @@
 #include "kf_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <thread>
 #include <vector>
 
@@ -678,6 +680,14 @@ template <class R> inline V3<R> uniformSphereSampling(Rng& rng, uint32_t purpose
     return p;
 }
 
+template <class R> inline void diskSampling(Rng& rng, uint32_t purpose, R& qx, R& qy) { // Sampling.glsl:124-134
+    do {
+        R a = (R)rng.next(purpose), b = (R)rng.next(purpose);
+        qx = R(2) * a - R(1);
+        qy = R(2) * b - R(1);
+    } while (qx * qx + qy * qy >= R(1));
+}
+
 // ---------------------------------------------------------------------------
 // Closest-hit shader (PathTrace.rchit).
 // ---------------------------------------------------------------------------
@@ -966,8 +976,12 @@ void closestHit(Ctx& cx, Rng& rng, Payload<R>& ray, const HitRec& h, const float
         }
     }
     Shading<R> sh{f, a2, diffuseColor, specularColor, transmissionColor, isInside};
-    ray.shadow_color = traceDirectionalLight(cx, rng, ray, worldPos, N, sh) +
-                       tracePointLights(cx, rng, ray, worldPos, N, sh) + traceActiveLights(cx, rng, ray, worldPos, N, sh);
+    // rchit:457-460 sums the three light loops; with kuafu's single tea/lcg stream their
+    // order matters, and it is the left-to-right order glslang emits
+    const V3<R> dir_part = traceDirectionalLight(cx, rng, ray, worldPos, N, sh);
+    const V3<R> point_part = tracePointLights(cx, rng, ray, worldPos, N, sh);
+    const V3<R> active_part = traceActiveLights(cx, rng, ray, worldPos, N, sh);
+    ray.shadow_color = dir_part + point_part + active_part;
     ray.origin = worldPos;
     ray.direction = L;
     ray.emission = V3<R>(R(0));
@@ -1007,13 +1021,9 @@ void render_pixel(Ctx& cx, const kf_oracle_view& view, uint32_t px, uint32_t py,
         R aperture = (R)cam.position[3];
         R focusDistance = (R)cam.front[3];
         R offx = 0, offy = 0;
-        if (view.rng_mode == KF_ORACLE_RNG_TEA_LCG || aperture > R(0)) { // diskSampling (Sampling.glsl:124-134)
+        if (view.rng_mode == KF_ORACLE_RNG_TEA_LCG || aperture > R(0)) {
             R qx, qy;
-            do {
-                R a = (R)rng.next(KF_RNG_LENS), b = (R)rng.next(KF_RNG_LENS);
-                qx = R(2) * a - R(1);
-                qy = R(2) * b - R(1);
-            } while (qx * qx + qy * qy >= R(1));
+            diskSampling<R>(rng, KF_RNG_LENS, qx, qy);
             offx = aperture / R(2) * qx;
             offy = aperture / R(2) * qy;
         }
@@ -1300,5 +1310,177 @@ void kf_oracle_camera_ubo(const float position[3], const float front[3], const f
 }
 
 uint8_t kf_oracle_srgb8(float linear) { return srgb_encode8(linear); }
+
+void kf_oracle_perpendicular(const float u[3], float out[3]) {
+    V3<float> r = getPerpendicularVector(V3<float>(u[0], u[1], u[2]));
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+void kf_oracle_uniform_sphere_lcg(uint32_t* state, float out[3]) {
+    Rng rng;
+    rng.mode = KF_ORACLE_RNG_TEA_LCG;
+    rng.ray_seed = *state;
+    V3<float> p = uniformSphereSampling<float>(rng, 0);
+    *state = rng.ray_seed;
+    out[0] = p.x; out[1] = p.y; out[2] = p.z;
+}
+void kf_oracle_disk_lcg(uint32_t* state, float out[2]) {
+    Rng rng;
+    rng.mode = KF_ORACLE_RNG_TEA_LCG;
+    rng.ray_seed = *state;
+    diskSampling<float>(rng, 0, out[0], out[1]);
+    *state = rng.ray_seed;
+}
+
+// The icosphere of the benchmark scenes: the icosahedron (golden-ratio vertices, 20 faces),
+// every face split into four `level` times with edge midpoints pushed to the unit sphere
+// (in double), then Geometry::recalculateNormals (geometry.cpp:268-295): the unit face
+// normals summed per vertex in face order (degenerate faces skipped) and renormalised, in
+// float, with glm::normalize = v * (1 / length(v)). uv are the spherical angles.
+int kf_oracle_icosphere(int level, kf_vertex* v, uint32_t vcap, uint32_t* idx, uint32_t icap, uint32_t* nv,
+                        uint32_t* ni) {
+    if (level < 0 || level > 8 || !nv || !ni) return 1;
+    const double g = (1.0 + std::sqrt(5.0)) / 2.0;
+    std::vector<std::array<double, 3>> P = {{-1, g, 0}, {1, g, 0},   {-1, -g, 0}, {1, -g, 0},
+                                            {0, -1, g}, {0, 1, g},   {0, -1, -g}, {0, 1, -g},
+                                            {g, 0, -1}, {g, 0, 1},   {-g, 0, -1}, {-g, 0, 1}};
+    auto unit = [](std::array<double, 3> p) {
+        const double n = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        return std::array<double, 3>{p[0] / n, p[1] / n, p[2] / n};
+    };
+    for (auto& p : P) p = unit(p);
+    std::vector<uint32_t> F = {0, 11, 5, 0, 5, 1, 0, 1, 7, 0, 7, 10, 0, 10, 11, 1, 5, 9, 5, 11, 4, 11, 10, 2,
+                               10, 7, 6, 7, 1, 8, 3, 9, 4, 3, 4, 2, 3, 2, 6, 3, 6, 8, 3, 8, 9, 4, 9, 5,
+                               2, 4, 11, 6, 2, 10, 8, 6, 7, 9, 8, 1};
+    for (int l = 0; l < level; ++l) {
+        std::map<uint64_t, uint32_t> mids;
+        auto mid = [&](uint32_t a, uint32_t b) -> uint32_t {
+            const uint64_t key = ((uint64_t)std::min(a, b) << 32) | std::max(a, b);
+            auto it = mids.find(key);
+            if (it != mids.end()) return it->second;
+            P.push_back(unit({(P[a][0] + P[b][0]) * 0.5, (P[a][1] + P[b][1]) * 0.5, (P[a][2] + P[b][2]) * 0.5}));
+            return mids[key] = (uint32_t)P.size() - 1;
+        };
+        std::vector<uint32_t> next;
+        next.reserve(F.size() * 4);
+        for (size_t f = 0; f < F.size(); f += 3) {
+            const uint32_t a = F[f], b = F[f + 1], c = F[f + 2];
+            const uint32_t ab = mid(a, b), bc = mid(b, c), ca = mid(c, a);
+            const uint32_t sub[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
+            next.insert(next.end(), sub, sub + 12);
+        }
+        F.swap(next);
+    }
+    *nv = (uint32_t)P.size();
+    *ni = (uint32_t)F.size();
+    if (vcap == 0 && icap == 0) return 0;
+    if (!v || !idx || vcap < P.size() || icap < F.size()) return 2;
+    const double pi = 3.14159265358979323846;
+    for (size_t i = 0; i < P.size(); ++i) {
+        kf_vertex& o = v[i];
+        std::memset(&o, 0, sizeof(o));
+        for (int k = 0; k < 3; ++k) o.pos[k] = (float)P[i][k];
+        o.uv[0] = (float)(0.5 + std::atan2(P[i][1], P[i][0]) / (2.0 * pi));
+        o.uv[1] = (float)(0.5 - std::asin(std::max(-1.0, std::min(1.0, P[i][2]))) / pi);
+    }
+    auto normalize = [](V3<float> a) { const float inv = 1.0f / std::sqrt(dot(a, a)); return a * inv; };
+    for (size_t f = 0; f < F.size(); f += 3) {
+        kf_vertex& A = v[F[f]];
+        kf_vertex& B = v[F[f + 1]];
+        kf_vertex& C = v[F[f + 2]];
+        const V3<float> pa(A.pos[0], A.pos[1], A.pos[2]), pb(B.pos[0], B.pos[1], B.pos[2]),
+            pc(C.pos[0], C.pos[1], C.pos[2]);
+        const V3<float> n = normalize(cross(pb - pa, pc - pa));
+        if (std::isnan(n.x)) continue;
+        for (kf_vertex* q : {&A, &B, &C}) {
+            q->normal[0] += n.x;
+            q->normal[1] += n.y;
+            q->normal[2] += n.z;
+        }
+    }
+    for (size_t i = 0; i < P.size(); ++i) {
+        V3<float> n(v[i].normal[0], v[i].normal[1], v[i].normal[2]);
+        if (n.x == 0.0f && n.y == 0.0f && n.z == 0.0f) continue;
+        n = normalize(n);
+        v[i].normal[0] = n.x; v[i].normal[1] = n.y; v[i].normal[2] = n.z;
+    }
+    std::memcpy(idx, F.data(), F.size() * sizeof(uint32_t));
+    return 0;
+}
+
+int kf_oracle_instance_rows(const float m[16], float rows[12]) {
+    double A[3][3], t[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) A[r][c] = m[c * 4 + r];
+        t[r] = m[12 + r];
+    }
+    // adjugate / determinant of the linear part, then -A^-1 t for the translation
+    const double c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+    const double c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+    const double c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    const double det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+    if (det == 0.0 || !std::isfinite(det)) return 1;
+    double I[3][3];
+    I[0][0] = c00 / det;
+    I[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / det;
+    I[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / det;
+    I[1][0] = c01 / det;
+    I[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) / det;
+    I[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / det;
+    I[2][0] = c02 / det;
+    I[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / det;
+    I[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / det;
+    for (int r = 0; r < 3; ++r) {
+        rows[r * 4 + 0] = (float)I[r][0];
+        rows[r * 4 + 1] = (float)I[r][1];
+        rows[r * 4 + 2] = (float)I[r][2];
+        rows[r * 4 + 3] = (float)(-(I[r][0] * t[0] + I[r][1] * t[1] + I[r][2] * t[2]));
+    }
+    return 0;
+}
+
+void kf_oracle_light_ubos(const float* dir, const float* points, uint32_t num_points, const float* actives,
+                          uint32_t num_actives, uint32_t num_textures, kf_dir_light_ubo* d, kf_point_lights_ubo* p,
+                          kf_active_lights_ubo* a) {
+    std::memset(d, 0, sizeof(*d));
+    std::memset(p, 0, sizeof(*p));
+    std::memset(a, 0, sizeof(*a));
+    if (dir) {  // direction = {normalize(direction), softness}, rgbs = {color, strength}
+        const V3<float> dv(dir[0], dir[1], dir[2]);
+        const float inv = 1.0f / std::sqrt(dot(dv, dv));
+        d->direction[0] = dv.x * inv; d->direction[1] = dv.y * inv; d->direction[2] = dv.z * inv;
+        d->direction[3] = dir[7];
+        d->rgbs[0] = dir[3]; d->rgbs[1] = dir[4]; d->rgbs[2] = dir[5]; d->rgbs[3] = dir[6];
+    }
+    for (uint32_t i = 0; i < KF_MAX_POINT_LIGHTS && i < num_points; ++i) {
+        const float* l = points + (size_t)i * 8;
+        p->posr[i][0] = l[0]; p->posr[i][1] = l[1]; p->posr[i][2] = l[2]; p->posr[i][3] = l[6];
+        p->rgbs[i][0] = l[3]; p->rgbs[i][1] = l[4]; p->rgbs[i][2] = l[5]; p->rgbs[i][3] = l[7];
+    }
+    for (uint32_t i = 0; i < KF_MAX_ACTIVE_LIGHTS && i < num_actives; ++i) {
+        const float* l = actives + (size_t)i * 24;
+        double vd[16], vi[16];
+        for (int k = 0; k < 16; ++k) vd[k] = l[k];
+        inverse4(vd, vi);  // glm::inverse(viewMat), in double rounded to float
+        float inv[16];
+        for (int k = 0; k < 16; ++k) inv[k] = (float)vi[k];
+        std::memcpy(a->view[i], l, sizeof(float) * 16);
+        // glm::perspective(fov, 1, 0.01, 1000): right-handed, clip depth [-1, 1]
+        const float fov = l[19], zn = 0.01f, zf = 1000.0f, aspect = 1.0f;
+        const float th = std::tan(fov / 2.0f);
+        float* P = a->proj[i];
+        P[0] = 1.0f / (aspect * th);
+        P[5] = 1.0f / th;
+        P[10] = -(zf + zn) / (zf - zn);
+        P[11] = -1.0f;
+        P[14] = -(2.0f * zf * zn) / (zf - zn);
+        a->front[i][0] = -inv[8]; a->front[i][1] = -inv[9]; a->front[i][2] = -inv[10]; a->front[i][3] = 1.0f;
+        a->rgbs[i][0] = l[16]; a->rgbs[i][1] = l[17]; a->rgbs[i][2] = l[18]; a->rgbs[i][3] = l[20];
+        a->position[i][0] = inv[12]; a->position[i][1] = inv[13]; a->position[i][2] = inv[14];
+        const int tex = (int)l[22];
+        a->sftp[i][0] = l[21];
+        a->sftp[i][1] = fov;
+        a->sftp[i][2] = (tex >= 0 && (uint32_t)tex < num_textures) ? (float)tex : -1.0f;
+    }
+}
 
 } // extern "C"

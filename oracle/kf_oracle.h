@@ -78,6 +78,10 @@ float kf_oracle_schlick(float cosine, float ior);
 float kf_oracle_ggx_d(float ndoth, float a2);
 float kf_oracle_g1(float d, float a2);
 void kf_oracle_schlick_fresnel(const float f0[3], float ldoth, float out[3]);
+void kf_oracle_perpendicular(const float u[3], float out[3]);          /* Random.glsl:58-65 */
+/* rejection samplers drawing from kuafu's lcg stream `*state` (advanced in place) */
+void kf_oracle_uniform_sphere_lcg(uint32_t* state, float out[3]);      /* Sampling.glsl:72-83 */
+void kf_oracle_disk_lcg(uint32_t* state, float out[2]);                /* Sampling.glsl:124-134 */
 
 /* Host-side camera math (src/core/camera.cpp:92-124, scene.cpp:236-250), FP64 inverses. */
 void kf_oracle_camera_ubo(const float position[3], const float front[3], const float up[3],
@@ -86,6 +90,23 @@ void kf_oracle_camera_ubo(const float position[3], const float front[3], const f
 
 /* sRGB encode of a linear value into an 8-bit code (the B8G8R8A8_SRGB frame, config.hpp:144). */
 uint8_t kf_oracle_srgb8(float linear);
+
+/* ---- scene construction, so a CPU render needs nothing of the product ---- */
+/* Unit icosphere of `level` subdivisions with smooth normals (Geometry::recalculateNormals,
+ * geometry.cpp:268-295) and spherical uv. Writes up to vcap vertices / icap indices; returns
+ * the counts in *nv / *ni (call with caps 0 to size the buffers). Returns 0 on success. */
+int kf_oracle_icosphere(int level, kf_vertex* v, uint32_t vcap, uint32_t* idx, uint32_t icap, uint32_t* nv,
+                        uint32_t* ni);
+/* gl_WorldToObjectEXT rows of a column-major object->world matrix (rt.cpp:127-137): the
+ * inverse affine map in FP64, rounded to float. Returns 0, or 1 for a singular matrix. */
+int kf_oracle_instance_rows(const float transform[16], float rows[12]);
+/* Scene::uploadLightBuffers (scene.cpp:252-292). dir: {direction xyz, color rgb, strength,
+ * softness} or NULL for no directional light; points: n x {position xyz, color rgb, radius,
+ * strength}; actives: n x {view (column-major 16), color rgb, fov, strength, softness,
+ * texID, pad}. texID outside [0, num_textures) reads as -1. */
+void kf_oracle_light_ubos(const float* dir, const float* points, uint32_t num_points, const float* actives,
+                          uint32_t num_actives, uint32_t num_textures, kf_dir_light_ubo* d, kf_point_lights_ubo* p,
+                          kf_active_lights_ubo* a);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,15 @@ def load():
             [C.POINTER(N.kf_camera_ubo)]
         L.kf_oracle_srgb8.restype = C.c_uint8
         L.kf_oracle_srgb8.argtypes = [C.c_float]
+        L.kf_oracle_perpendicular.argtypes = [C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3)]
+        L.kf_oracle_uniform_sphere_lcg.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_float * 3)]
+        L.kf_oracle_disk_lcg.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_float * 2)]
+        L.kf_oracle_icosphere.argtypes = [C.c_int, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32,
+                                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.kf_oracle_instance_rows.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.kf_oracle_light_ubos.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
+                                           C.POINTER(N.kf_dir_light_ubo), C.POINTER(N.kf_point_lights_ubo),
+                                           C.POINTER(N.kf_active_lights_ubo)]
         _lib = L
     return _lib
 

@@ -5,12 +5,10 @@ Sampling.glsl hold its RNG, BRDF and sampling helpers). There is no GLSL
 toolchain or graphics stack here, but these two files are plain arithmetic, so
 this script compiles them *as C++*:
 
-  * the files are read where they lie (REFERENCE/resources/shaders/base);
-  * a mechanical rewrite turns GLSL parameter qualifiers into C++
-    (``inout T x`` -> ``T& x``, ``in T x`` -> ``T x``) and drops ``#include``;
-  * a small compatibility header supplies vec2/vec3, the GLSL built-ins they
-    call and brace-initialised constructors, so constructor arguments are
-    evaluated left to right as GLSL evaluates them;
+  * the files are read where they lie (<kuafu>/resources/shaders/base);
+  * the mechanical rewrite and compatibility header of tests/golden/glsl_cpp.py
+    (GLSL qualifiers to C++, vec2/vec3 and the built-ins, brace-initialised
+    constructors evaluating their arguments left to right as GLSL does);
   * g++ compiles with ``-fsingle-precision-constant`` (GLSL literals are float)
     and ``-ffp-contract=off``; sin / cos / pow(2, x) / pow(x, 5) come from the
     oracle's deterministic functions (the GLSL spec leaves their rounding to the
@@ -19,13 +17,12 @@ this script compiles them *as C++*:
 The program evaluates each helper on seeded inputs (drawing its uniforms with
 the shaders' own tea / lcg / rnd) and prints JSON, written next to this script.
 The result is committed; tests/test_oracle.py compares the oracle against it.
-Run from the repository root:  python tests/golden/make_shader_vectors.py
+Run from the repository root with the kuafu checkout:
+  python tests/golden/make_shader_vectors.py <path-to-kuafu>   (or $KF_REFERENCE)
 """
 from __future__ import annotations
 
 import json
-import os
-import re
 import subprocess
 import sys
 import tempfile
@@ -33,61 +30,9 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REFERENCE = Path(os.environ.get("KF_REFERENCE", "/root/reference"))
-SHADERS = REFERENCE / "resources" / "shaders" / "base"
+sys.path.insert(0, str(HERE))
 
-COMPAT = r"""
-#include <cmath>
-#include <cstdint>
-#include <cstdio>
-#undef M_PI
-typedef uint32_t uint;
-extern "C" float kf_oracle_sin(float);
-extern "C" float kf_oracle_cos(float);
-extern "C" float kf_oracle_exp2(float);
-namespace glsl {
-struct vec2_t { float x, y;
-  vec2_t() : x(0), y(0) {}
-  vec2_t(float a) : x(a), y(a) {}
-  vec2_t(float a, float b) : x(a), y(b) {} };
-struct vec3_t { float x, y, z;
-  vec3_t() : x(0), y(0), z(0) {}
-  vec3_t(float a) : x(a), y(a), z(a) {}
-  vec3_t(float a, float b, float c) : x(a), y(b), z(c) {} };
-inline vec2_t operator*(float s, vec2_t v) { return vec2_t(s * v.x, s * v.y); }
-inline vec2_t operator-(vec2_t v, float s) { return vec2_t(v.x - s, v.y - s); }
-inline vec3_t operator+(vec3_t a, vec3_t b) { return vec3_t(a.x + b.x, a.y + b.y, a.z + b.z); }
-inline vec3_t operator-(vec3_t a, vec3_t b) { return vec3_t(a.x - b.x, a.y - b.y, a.z - b.z); }
-inline vec3_t operator-(vec3_t a) { return vec3_t(-a.x, -a.y, -a.z); }
-inline vec3_t operator*(vec3_t a, vec3_t b) { return vec3_t(a.x * b.x, a.y * b.y, a.z * b.z); }
-inline vec3_t operator*(vec3_t a, float s) { return vec3_t(a.x * s, a.y * s, a.z * s); }
-inline vec3_t operator*(float s, vec3_t a) { return vec3_t(s * a.x, s * a.y, s * a.z); }
-inline vec3_t operator/(vec3_t a, float s) { return vec3_t(a.x / s, a.y / s, a.z / s); }
-inline vec3_t operator-(vec3_t a, float s) { return vec3_t(a.x - s, a.y - s, a.z - s); }
-inline float dot(vec2_t a, vec2_t b) { return a.x * b.x + a.y * b.y; }
-inline float dot(vec3_t a, vec3_t b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline vec3_t cross(vec3_t a, vec3_t b) { return vec3_t(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
-inline float abs(float x) { return std::fabs(x); }
-inline vec3_t abs(vec3_t v) { return vec3_t(std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)); }
-inline float sqrt(float x) { return std::sqrt(x); }
-inline float max(float a, float b) { return std::fmax(a, b); }
-inline float min(float a, float b) { return std::fmin(a, b); }
-inline float clamp(float x, float lo, float hi) { return min(max(x, lo), hi); }
-inline float sin(float x) { return kf_oracle_sin(x); }
-inline float cos(float x) { return kf_oracle_cos(x); }
-inline float pow(float x, float y) {
-  if (x == 2.0f) return kf_oracle_exp2(y);
-  if (y == 5.0f) { float x2 = x * x; return (x2 * x2) * x; }
-  return std::pow(x, y); }
-inline float length(vec3_t v) { return sqrt(dot(v, v)); }
-inline vec3_t normalize(vec3_t v) { float inv = 1.0f / length(v); return v * inv; }
-}
-using namespace glsl;
-#define vec2(...) (glsl::vec2_t{__VA_ARGS__})
-#define vec3(...) (glsl::vec3_t{__VA_ARGS__})
-typedef glsl::vec2_t vec2;
-typedef glsl::vec3_t vec3;
-"""
+import glsl_cpp  # noqa: E402
 
 DRIVER = r"""
 static void pv(const char* k, vec3 v) { std::printf("\"%s\": [%.9g, %.9g, %.9g]", k, v.x, v.y, v.z); }
@@ -130,26 +75,53 @@ int main() {
     std::printf("%s{\"u0\": %.9g, \"u1\": %.9g, ", i ? ", " : "", u0, u1);
     pv("n", n); std::printf(", "); pv("out", d); std::printf("}");
   }
+  std::printf("],\n\"schlick_fresnel\": [");
+  for (int i = 0; i < 64; ++i) {
+    vec3 f0 = vec3(rnd(s), rnd(s), rnd(s));
+    float ldoth = rnd(s);
+    std::printf("%s{\"ldoth\": %.9g, ", i ? ", " : "", ldoth);
+    pv("f0", f0); std::printf(", "); pv("out", schlickFresnel(f0, ldoth)); std::printf("}");
+  }
+  std::printf("],\n\"perpendicular\": [");
+  for (int i = 0; i < 64; ++i) {
+    vec3 u = vec3(2.0f * rnd(s) - 1.0f, 2.0f * rnd(s) - 1.0f, 2.0f * rnd(s) - 1.0f);
+    if (i % 8 == 1) u.y = u.x;        // ties between components
+    if (i % 8 == 2) u.z = -u.x;
+    std::printf("%s{", i ? ", " : "");
+    pv("u", u); std::printf(", "); pv("out", getPerpendicularVector(u)); std::printf("}");
+  }
+  std::printf("],\n\"uniform_sphere\": [");
+  for (int i = 0; i < 64; ++i) {
+    uint st = s * 747796405u + (uint)i, before = st;
+    vec3 p = uniformSphereSampling(st);
+    std::printf("%s{\"state\": %u, \"state_after\": %u, ", i ? ", " : "", before, st);
+    pv("out", p); std::printf("}");
+  }
+  std::printf("],\n\"disk\": [");
+  for (int i = 0; i < 64; ++i) {
+    uint st = s * 2891336453u + (uint)i, before = st;
+    vec2 p = diskSampling(st);
+    std::printf("%s{\"state\": %u, \"state_after\": %u, \"out\": [%.9g, %.9g]}", i ? ", " : "", before, st,
+                p.x, p.y);
+  }
+  std::printf("],\n\"lcg\": [");
+  for (int i = 0; i < 64; ++i) {
+    uint st = (uint)i * 2246822519u + 3266489917u, before = st;
+    uint a = lcg(st);
+    float r = rnd(st);
+    std::printf("%s{\"state\": %u, \"lcg\": %u, \"rnd\": %.9g, \"state_after\": %u}", i ? ", " : "", before,
+                a, r, st);
+  }
   std::printf("]\n}\n");
   return 0;
 }
 """
 
 
-def glsl_to_cpp(text: str) -> str:
-    text = re.sub(r'^\s*#\s*include\s+"[^"]*"\s*$', "", text, flags=re.M)
-    text = re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1 &\2", text)
-    text = re.sub(r"([(,]\s*)in\s+(\w+)\s+(\w+)", r"\1\2 \3", text)
-    return text
-
-
-def main() -> int:
-    rnd = SHADERS / "Random.glsl"
-    smp = SHADERS / "Sampling.glsl"
-    if not rnd.exists():
-        print(f"kuafu shaders not found under {SHADERS}", file=sys.stderr)
-        return 1
-    src = COMPAT + glsl_to_cpp(rnd.read_text()) + glsl_to_cpp(smp.read_text()) + DRIVER
+def main(argv) -> int:
+    shaders = glsl_cpp.reference_root(argv[1] if len(argv) > 1 else None) / "resources" / "shaders" / "base"
+    src = (glsl_cpp.COMPAT + glsl_cpp.glsl_to_cpp((shaders / "Random.glsl").read_text()) +
+           glsl_cpp.glsl_to_cpp((shaders / "Sampling.glsl").read_text()) + DRIVER)
     oracle_lib = ROOT / "oracle" / "liboracle.so"
     if not oracle_lib.exists():
         sys.path.insert(0, str(ROOT))
@@ -172,4 +144,4 @@ def main() -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv))

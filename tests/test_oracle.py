@@ -3,9 +3,11 @@
 kuafu ships no tests or golden vectors for its render path; the oracle is pinned
 by (1) the Philox4x32-10 known-answer vectors of Random123 (Salmon et al.,
 SC'11), (2) golden vectors in tests/golden/ generated by compiling kuafu's own
-GLSL shader library as C++ (tests/golden/make_shader_vectors.py), (3) closed-form
-checks of every shader helper against float64 formulas, and (4) watertightness /
-BVH-equivalence properties of the traversal.
+GLSL shader library as C++ (tests/golden/make_shader_vectors.py), matched
+exactly, (3) closed-form checks of every shader helper against float64 formulas,
+and (4) watertightness / BVH-equivalence properties of the traversal. The whole
+bounce loop is checked against kuafu's compiled ray-tracing shaders in
+tests/test_oracle_pipeline.py.
 """
 import json
 import math
@@ -209,29 +211,59 @@ def test_srgb_encode_matches_formula():
 
 
 def test_golden_shader_vectors():
-    """Outputs of kuafu's own GLSL helpers (Random.glsl / Sampling.glsl compiled as C++)."""
+    """Outputs of kuafu's own GLSL helpers (Random.glsl / Sampling.glsl compiled as C++, the
+    same operations in the same order): the oracle must reproduce every one exactly. JSON
+    holds each float32 result with 9 significant digits, which round-trips to the float."""
     path = GOLDEN / "shader_vectors.json"
     if not path.exists():
-        pytest.skip("golden vectors not generated")
+        pytest.fail("tests/golden/shader_vectors.json is missing: run tests/golden/make_shader_vectors.py")
     import ctypes as C
 
     L = O.load()
     g = json.loads(path.read_text())
+    F = np.float32
+    v3 = lambda out: [F(x) for x in out[:]]
+    want3 = lambda xs: [F(x) for x in xs]
     for case in g["tea"]:
         assert L.kf_oracle_tea(case["v0"], case["v1"]) == case["out"]
     for case in g["schlick"]:
-        assert L.kf_oracle_schlick(case["cos"], case["ior"]) == pytest.approx(case["out"], rel=2e-6, abs=1e-9)
+        assert F(L.kf_oracle_schlick(case["cos"], case["ior"])) == F(case["out"])
     for case in g["ggx_d"]:
-        assert L.kf_oracle_ggx_d(case["ndoth"], case["a2"]) == pytest.approx(case["out"], rel=2e-6)
+        assert F(L.kf_oracle_ggx_d(case["ndoth"], case["a2"])) == F(case["out"])
     for case in g["g1"]:
-        assert L.kf_oracle_g1(case["d"], case["a2"]) == pytest.approx(case["out"], rel=2e-6)
+        assert F(L.kf_oracle_g1(case["d"], case["a2"])) == F(case["out"])
     for case in g["sample_ggx"]:
         nn = (C.c_float * 3)(*case["n"])
         out = (C.c_float * 3)()
         L.kf_oracle_sample_ggx(case["u0"], case["u1"], case["a2"], C.byref(nn), C.byref(out))
-        assert np.allclose(out[:], case["out"], atol=2e-6)
+        assert v3(out) == want3(case["out"])
     for case in g["cosine"]:
         nn = (C.c_float * 3)(*case["n"])
         out = (C.c_float * 3)()
         L.kf_oracle_cosine_hemisphere(case["u0"], case["u1"], C.byref(nn), C.byref(out))
-        assert np.allclose(out[:], case["out"], atol=2e-6)
+        assert v3(out) == want3(case["out"])
+    for case in g["schlick_fresnel"]:
+        f0 = (C.c_float * 3)(*case["f0"])
+        out = (C.c_float * 3)()
+        L.kf_oracle_schlick_fresnel(C.byref(f0), case["ldoth"], C.byref(out))
+        assert v3(out) == want3(case["out"])
+    for case in g["perpendicular"]:
+        u = (C.c_float * 3)(*case["u"])
+        out = (C.c_float * 3)()
+        L.kf_oracle_perpendicular(C.byref(u), C.byref(out))
+        assert v3(out) == want3(case["out"])
+    for case in g["uniform_sphere"]:
+        st = C.c_uint32(case["state"])
+        out = (C.c_float * 3)()
+        L.kf_oracle_uniform_sphere_lcg(C.byref(st), C.byref(out))
+        assert v3(out) == want3(case["out"]) and st.value == case["state_after"]
+    for case in g["disk"]:
+        st = C.c_uint32(case["state"])
+        out = (C.c_float * 2)()
+        L.kf_oracle_disk_lcg(C.byref(st), C.byref(out))
+        assert [F(x) for x in out[:]] == want3(case["out"]) and st.value == case["state_after"]
+    for case in g["lcg"]:
+        st = C.c_uint32(case["state"])
+        got = L.kf_oracle_rnd_lcg(C.byref(st))  # one lcg step, as rnd
+        assert F(got) == F((case["lcg"] & 0xFFFFFF) / float(1 << 24))
+        assert F(L.kf_oracle_rnd_lcg(C.byref(st))) == F(case["rnd"]) and st.value == case["state_after"]
