@@ -10,13 +10,14 @@ issued; BVH build is outside the timed region.
 
 The line also carries "time_to_relmse": the Cornell box at 1920x1080, the learned
 denoiser (trained first on this renderer's own low/high-spp pairs) against plain
-accumulation, time until relMSE <= 1e-3 against a 4096-spp FP64 reference
-(kuafu_gb300/denoise_eval.py; --no-denoise skips it).
+accumulation, both measured until relMSE <= 1e-3 against a 40960-spp FP64
+reference (kuafu_gb300/denoise_eval.py; --no-denoise skips it; N = 1 only).
 
 Under torchrun (N > 1) every rank renders its own replica of the workload (the
 path has no cross-GPU exchange); value = rays of all ranks / max time over ranks.
 --impl reference times the CPU implementation (the oracle port of kuafu's
-shaders) on the host cores over a bounded crop of the same workload.
+shaders) on the host cores over a bounded crop of the same workload, with the
+scene flattened on the oracle side: that arm maps no library of this package.
 """
 from __future__ import annotations
 
@@ -153,7 +154,8 @@ def cpu_baseline_sample(seconds_target=12.0, threads=0):
 
 def time_to_relmse_summary() -> dict:
     """Second half of the metric: time to relMSE <= 1e-3 at 1920x1080 (Cornell box, depth 5),
-    learned denoiser vs plain accumulation, one GPU (kuafu_gb300.denoise_eval)."""
+    learned denoiser vs plain accumulation, one GPU (kuafu_gb300.denoise_eval). Both arms
+    are measured (no extrapolation) against a 40960-spp FP64 reference."""
     from kuafu_gb300 import denoise_eval
 
     t0 = time.perf_counter()
@@ -173,14 +175,16 @@ def time_to_relmse_summary() -> dict:
         "relmse": "mean (x - ref)^2 / (ref^2 + 1e-2) over pixels and rgb, FP64 on the GPU",
         "reference": res["reference"],
         "headline_tau": 1e-3,
-        "headline": head,
+        "headline": head["relmse"],
+        "headline_debiased": head["relmse_debiased"],
         "thresholds": res["time_to_relmse"],
-        "plain_fit": res["plain_fit"],
         "plain": res["plain"],
+        "plain_ms_per_spp": res["plain_fit"]["ms_per_spp"],
         "denoised": [{k: d[k] for k in ("spp", "ms", "render_ms", "denoise_ms", "relmse", "relmse_debiased")}
                      for d in res["denoised"]],
         "training": {k: v for k, v in res["training"].items() if k != "loss_curve"},
         "loss_first_last": [res["training"]["loss_curve"][0], res["training"]["loss_curve"][-1]],
+        "note_4096spp_reference": res["note_4096spp_reference"],
         "denoiser_roofline": {"bound": "tensor", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s",
                               "frac": (ach / peak_tf) if peak_tf else None,
                               "flops_per_frame": res["denoiser_flops_per_frame"],
@@ -483,9 +487,10 @@ def run_ours(args):
             except Exception:
                 traffic = None
         cpu = cpu_baseline_sample()
-        ttr = None if args.no_denoise else time_to_relmse_summary()
-        batched = None if args.no_batch else batched_summary(device)
-        active = None if args.no_batch else active_light_summary(device)
+        # single-GPU experiments: run once, at N = 1 (under torchrun the other ranks would idle)
+        ttr = None if (args.no_denoise or ws > 1) else time_to_relmse_summary()
+        batched = None if (args.no_batch or ws > 1) else batched_summary(device)
+        active = None if (args.no_batch or ws > 1) else active_light_summary(device)
         result = {
             "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -223,6 +223,244 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
     if (warp == 0) tc::tmem_dealloc(tmem, p.tmem_cols);
 }
 
+// ---------------------------------------------------------------------------
+// Halo convolution: persistent, warp-specialised, for images at least one tile wide.
+//
+// A tile is R output rows x 128 pixels x n_tile output channels: R accumulators of
+// n_tile TMEM columns, double-buffered so the epilogue of one tile overlaps the MMAs of
+// the next. Per chunk of CK input channels one 5D TMA box brings the tile's input halo,
+// (R + 2) rows x 130 pixels, into shared memory as [row][channel group][pixel][8
+// channels]: a K-major operand without swizzle (8 pixels x 16 bytes per core matrix,
+// core matrices 128 bytes apart along M and 130 x 16 bytes apart along K). The A
+// operand of tap (dy, dx) for output row r is that buffer viewed from row r + dy + 1,
+// pixel dx + 1 on: a descriptor offset, so the halo is read from L2 once per chunk
+// and used by all 9 taps (the per-tap kernel above reads 9 shifted boxes). The
+// weights of a chunk ([tap][n_tile][CK], swizzled rows of CK channels) stream with the
+// halo, or, when one chunk covers all input channels, are loaded once per CTA.
+//
+// Warp 0 lane 0: TMA producer (kHaloStages-deep ring). Warp 1 lane 0: MMA issuer.
+// Warps 2-5: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels.
+// Every wait is bounded; on expiry the kernel records an error code, lets its own
+// copies and MMAs finish and frees its TMEM.
+// ---------------------------------------------------------------------------
+constexpr int kHaloW = 130;     // 128 output pixels + 2 halo pixels
+constexpr int kHaloStages = 3;
+constexpr int kHaloThreads = 192;
+
+struct HaloParams {
+    int N, H, W, Cin, Cout;
+    int n_tile, R, kchunks;
+    int tiles_x, tiles_y, num_tiles;
+    int w_resident;          // 1: the weights of all input channels are one chunk, loaded once
+    uint32_t halo_bytes;     // bytes of one halo box
+    uint32_t halo_stride;    // its slot in shared memory (1024-aligned)
+    uint32_t w_bytes;        // bytes of one chunk of weights (9 x n_tile x CK)
+    uint32_t w_stride;
+    uint32_t tmem_cols;
+    const float* bias;
+    int relu;
+    __nv_bfloat16* out;
+    int out_cstride, out_coff;
+    float* outf;
+};
+
+template <int CK>
+__global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_constant__ CUtensorMap tmX,
+                                                                 const __grid_constant__ CUtensorMap tmW,
+                                                                 const HaloParams p) {
+    constexpr int G = CK / 8;                          // 16-byte channel groups per chunk
+    constexpr uint32_t W_ROW = CK * 2;                 // bytes per weight row (the swizzle width)
+    constexpr uint32_t W_LAYOUT = CK == 32 ? 4u : 6u;  // 64 B / 32 B swizzle
+    constexpr uint32_t ROW_BYTES = kHaloW * 16;        // one channel group of one halo row
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* halo = smem;
+    uint8_t* wst = halo + kHaloStages * p.halo_stride;
+    const int w_slots = p.w_resident ? 1 : kHaloStages;
+    uint64_t* full = reinterpret_cast<uint64_t*>(wst + w_slots * p.w_stride);
+    uint64_t* empty = full + kHaloStages;
+    uint64_t* acc_full = empty + kHaloStages;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* wbar = acc_empty + 2;
+    uint64_t* mma_done = wbar + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+    float* sbias = reinterpret_cast<float*>(tmem_slot + 4);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.y * p.n_tile;
+    const int acc_cols = p.R * p.n_tile;
+
+    if (warp == 0) tc::tmem_alloc(tmem_slot, p.tmem_cols);
+    for (int i = threadIdx.x; i < p.n_tile; i += blockDim.x)
+        sbias[i] = (p.bias && n0 + i < p.Cout) ? p.bias[n0 + i] : 0.0f;
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < kHaloStages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 4);
+        }
+        tc::mbar_init(wbar, 1);
+        tc::mbar_init(mma_done, 1);
+        tc::fence_barrier_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    auto tile_origin = [&](int t, int& n_img, int& y0, int& x0) {
+        const int per_img = p.tiles_x * p.tiles_y;
+        n_img = t / per_img;
+        const int r = t % per_img;
+        y0 = (r / p.tiles_x) * p.R;
+        x0 = (r % p.tiles_x) * 128;
+    };
+
+    if (warp == 0 && lane == 0) {
+        // ---- producer ----
+        bool ok = true;
+        if (p.w_resident) {
+            tc::mbar_arrive_expect_tx(wbar, p.w_bytes);
+            tc::tma_load_3d(wst, &tmW, wbar, 0, n0, 0);
+        }
+        uint32_t it = 0;
+        for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
+            int n_img, y0, x0;
+            tile_origin(t, n_img, y0, x0);
+            for (int c = 0; c < p.kchunks; ++c, ++it) {
+                const uint32_t s = it % kHaloStages;
+                if (it >= (uint32_t)kHaloStages &&
+                    !tc::mbar_wait(&empty[s], ((it / kHaloStages) - 1) & 1, kWaitBudget)) {
+                    set_error(11);
+                    ok = false;
+                    break;
+                }
+                tc::mbar_arrive_expect_tx(&full[s], p.halo_bytes + (p.w_resident ? 0u : p.w_bytes));
+                tc::tma_load_5d(halo + s * p.halo_stride, &tmX, &full[s], 0, x0 - 1, c * G, y0 - 1, n_img);
+                if (!p.w_resident) tc::tma_load_3d(wst + s * p.w_stride, &tmW, &full[s], c * CK, n0, 0);
+            }
+        }
+        // drain: every issued copy must have landed before the CTA may exit
+        for (uint32_t s = 0; s < (uint32_t)kHaloStages && s < it; ++s) {
+            const uint32_t last = ((it - 1 - s) / kHaloStages) * kHaloStages + s;
+            if (!tc::mbar_wait(&full[s], (last / kHaloStages) & 1, kWaitBudget)) set_error(12);
+        }
+        if (p.w_resident && !tc::mbar_wait(wbar, 0, kWaitBudget)) set_error(13);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        const uint32_t idesc = tc::idesc_bf16(128, (uint32_t)p.n_tile);
+        const uint32_t halo0 = tc::smem_u32(halo), w0 = tc::smem_u32(wst);
+        bool ok = !p.w_resident || tc::mbar_wait(wbar, 0, kWaitBudget);
+        if (!ok) set_error(14);
+        uint32_t it = 0, j = 0;
+        for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x, ++j) {
+            const uint32_t b = j & 1;
+            if (j >= 2 && !tc::mbar_wait(&acc_empty[b], ((j / 2) - 1) & 1, kWaitBudget)) {
+                set_error(15);
+                break;
+            }
+            tc::fence_after_sync();
+            const uint32_t acc = tmem + b * (uint32_t)acc_cols;
+            for (int c = 0; c < p.kchunks; ++c, ++it) {
+                const uint32_t s = it % kHaloStages;
+                if (!tc::mbar_wait(&full[s], (it / kHaloStages) & 1, kWaitBudget)) {
+                    set_error(16);
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t ha = halo0 + s * p.halo_stride;
+                const uint32_t wa = w0 + (p.w_resident ? 0u : s * p.w_stride);
+                for (int r = 0; r < p.R; ++r) {
+#pragma unroll
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const uint32_t row = (uint32_t)(r + tap / 3);  // halo row r + dy + 1
+#pragma unroll
+                        for (int kk = 0; kk < CK / 16; ++kk) {
+                            const uint64_t ad = tc::smem_desc_noswz(
+                                ha + (row * G + 2 * kk) * ROW_BYTES + (uint32_t)(tap % 3) * 16u, ROW_BYTES, 128u);
+                            const uint64_t bd = tc::smem_desc(wa + (uint32_t)tap * p.n_tile * W_ROW + kk * 32,
+                                                              8u * W_ROW, W_LAYOUT);
+                            tc::mma_bf16(acc + (uint32_t)(r * p.n_tile), ad, bd, idesc,
+                                         (c > 0 || tap > 0 || kk > 0) ? 1u : 0u);
+                        }
+                    }
+                }
+                tc::mma_commit(&empty[s]);
+            }
+            if (!ok) break;
+            tc::mma_commit(&acc_full[b]);
+        }
+        // every MMA of this CTA completes before the TMEM is freed
+        tc::mma_commit(mma_done);
+        if (!tc::mbar_wait(mma_done, 0, kWaitBudget)) set_error(17);
+    } else if (warp >= 2) {
+        // ---- epilogue ----
+        const int lg = warp & 3;                 // TMEM lane group of this warp
+        const int px_in_tile = lg * 32 + lane;
+        uint32_t j = 0;
+        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++j) {
+            const uint32_t b = j & 1;
+            const bool ready = tc::mbar_wait(&acc_full[b], (j / 2) & 1, kWaitBudget);
+            __syncwarp();
+            if (!ready) {
+                set_error(18);
+                break;
+            }
+            tc::fence_after_sync();
+            int n_img, y0, x0;
+            tile_origin(t, n_img, y0, x0);
+            const int px = x0 + px_in_tile;
+            for (int r = 0; r < p.R; ++r) {
+                const int py = y0 + r;
+                const bool valid = px < p.W && py < p.H;
+                const size_t base = ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
+                const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
+                for (int c = 0; c < p.n_tile; c += 16) {
+                    uint32_t r0[8], r1[8];
+                    tc::tmem_ld8(tmem + ((uint32_t)(lg * 32) << 16) + col0 + (uint32_t)c, r0);
+                    tc::tmem_ld8(tmem + ((uint32_t)(lg * 32) << 16) + col0 + (uint32_t)(c + 8), r1);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const uint32_t* rr = h ? r1 : r0;
+                        const int cc = c + 8 * h, co = n0 + cc;
+                        if (!valid || co >= p.Cout) continue;
+                        float v[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            v[q] = __uint_as_float(rr[q]) + sbias[cc + q];
+                            if (p.relu) v[q] = fmaxf(v[q], 0.0f);
+                        }
+                        if (p.outf) {
+                            for (int q = 0; q < 8 && co + q < p.Cout; ++q) p.outf[base + co + q] = v[q];
+                            continue;
+                        }
+                        __nv_bfloat16* dst = p.out + base + co;
+                        if (co + 8 <= p.Cout && ((p.out_coff + co) & 7) == 0 && (p.out_cstride & 7) == 0) {
+                            __nv_bfloat162 q2[4];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(q2);
+                        } else {
+                            for (int q = 0; q < 8 && co + q < p.Cout; ++q) dst[q] = __float2bfloat16_rn(v[q]);
+                        }
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, p.tmem_cols);
+}
+
 // ---- host: tensor maps ----
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -284,6 +522,106 @@ void launch_tc(dim3 grid, const CUtensorMap& a, const CUtensorMap& b, const TcPa
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
+// Shape of a halo-convolution launch: rows per tile R, channels per chunk CK, and the
+// shared memory it takes. Larger R first (less halo per output row, fewer weight
+// reloads per pixel), then larger CK; both accumulators must fit the 512 TMEM columns.
+struct HaloShape {
+    int R = 0, CK = 0;
+    bool w_resident = false;
+    uint32_t halo_bytes = 0, halo_stride = 0, w_bytes = 0, w_stride = 0;
+    size_t smem = 0;
+};
+
+bool halo_shape(int Cin, int n_tile, HaloShape& out) {
+    for (int R : {4, 2, 1}) {
+        if (2 * R * n_tile > 512) continue;
+        for (int CK : {32, 16}) {
+            if (Cin % CK) continue;
+            HaloShape h;
+            h.R = R;
+            h.CK = CK;
+            h.w_resident = Cin == CK;
+            h.halo_bytes = (uint32_t)((R + 2) * kHaloW * CK * 2);
+            h.halo_stride = (h.halo_bytes + 1023u) & ~1023u;
+            h.w_bytes = (uint32_t)(9 * n_tile * CK * 2);
+            h.w_stride = (h.w_bytes + 1023u) & ~1023u;
+            h.smem = 1024 + (size_t)kHaloStages * h.halo_stride +
+                     (size_t)(h.w_resident ? 1 : kHaloStages) * h.w_stride + 256 + 4u * (size_t)n_tile;
+            if (h.smem <= 227u * 1024u) {
+                out = h;
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+int num_sms() {
+    int dev = 0, n = 0;
+    KF_CUDA_CHECK(cudaGetDevice(&dev));
+    KF_CUDA_CHECK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    return std::max(1, n);
+}
+
+template <int CK> void launch_halo(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p,
+                                   size_t smem, cudaStream_t st) {
+    static bool configured = false;
+    if (!configured) {
+        KF_CUDA_CHECK(cudaFuncSetAttribute(k_conv_halo<CK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           227 * 1024));
+        configured = true;
+    }
+    k_conv_halo<CK><<<grid, kHaloThreads, smem, st>>>(x, w, p);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+
+// The halo kernel for images at least one 128-pixel tile wide; false when no shape fits.
+bool conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
+                  const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
+                  cudaStream_t st, float* y_f32) {
+    const int n_tile = Cout_rows <= 256 ? Cout_rows : 128;
+    HaloShape h;
+    if (W < 128 || !halo_shape(Cin, n_tile, h)) return false;
+    // input as [n][y][channel group][x][8 channels]: dims (8, W, Cin / 8, H, N)
+    const uint64_t xdims[5] = {8, (uint64_t)W, (uint64_t)Cin / 8, (uint64_t)H, (uint64_t)N};
+    const uint64_t xstr[4] = {(uint64_t)Cin * 2, 16, (uint64_t)W * Cin * 2, (uint64_t)H * W * Cin * 2};
+    const uint32_t xbox[5] = {8, (uint32_t)kHaloW, (uint32_t)h.CK / 8, (uint32_t)h.R + 2, 1};
+    const CUtensorMap mx = make_map(x, 5, xdims, xstr, xbox, CU_TENSOR_MAP_SWIZZLE_NONE);
+    const uint64_t wdims[3] = {(uint64_t)Cin, (uint64_t)Cout_rows, 9};
+    const uint64_t wstr[2] = {(uint64_t)Cin * 2, (uint64_t)Cout_rows * Cin * 2};
+    const uint32_t wbox[3] = {(uint32_t)h.CK, (uint32_t)n_tile, 9};
+    const CUtensorMap mw = make_map(w, 3, wdims, wstr, wbox,
+                                    h.CK == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    HaloParams p{};
+    p.N = N; p.H = H; p.W = W; p.Cin = Cin; p.Cout = Cout;
+    p.n_tile = n_tile;
+    p.R = h.R;
+    p.kchunks = Cin / h.CK;
+    p.tiles_x = (W + 127) / 128;
+    p.tiles_y = (H + h.R - 1) / h.R;
+    p.num_tiles = p.tiles_x * p.tiles_y * N;
+    p.w_resident = h.w_resident ? 1 : 0;
+    p.halo_bytes = h.halo_bytes;
+    p.halo_stride = h.halo_stride;
+    p.w_bytes = h.w_bytes;
+    p.w_stride = h.w_stride;
+    p.tmem_cols = pow2_at_least((uint32_t)(2 * h.R * n_tile));
+    p.bias = bias;
+    p.relu = relu ? 1 : 0;
+    p.out = y;
+    p.outf = y_f32;
+    p.out_cstride = y_cstride;
+    p.out_coff = y_coff;
+    const int slices = (Cout_rows + n_tile - 1) / n_tile;
+    const int per_slice = std::max(1, num_sms() / slices);
+    const dim3 grid((unsigned)std::min(p.num_tiles, per_slice), (unsigned)slices, 1);
+    if (h.CK == 32)
+        launch_halo<32>(grid, mx, mw, p, h.smem, st);
+    else
+        launch_halo<16>(grid, mx, mw, p, h.smem, st);
+    return true;
+}
+
 } // namespace
 
 void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
@@ -297,6 +635,8 @@ void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     KF_REQUIRE(y_coff >= 0 && y_coff + Cout <= y_cstride, KF_ERR_INVALID_ARGUMENT, "conv3x3: output slice");
     KF_REQUIRE(((uintptr_t)x & 15) == 0 && ((uintptr_t)w & 15) == 0, KF_ERR_INVALID_ARGUMENT,
                "conv3x3: tensors must be 16-byte aligned");
+    if (conv3x3_halo(x, N, H, W, Cin, w, Cout_rows, bias, Cout, relu, y, y_cstride, y_coff, st, y_f32)) return;
+    // narrow images: one CTA per tile of bw x bh = 128 pixels, 9 tap-shifted boxes per chunk
     int bw = 128;
     while (bw > W && bw > 8) bw >>= 1;
     const int bh = 128 / bw;

@@ -71,6 +71,18 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3, int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6, "
+        "%7}], [%2];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // ---- TMEM ----
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
@@ -118,6 +130,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo, uint3
     d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;   // stride byte offset
     d |= (uint64_t)1u << 46;                       // descriptor version (sm_100)
     d |= (uint64_t)(layout & 7u) << 61;            // swizzle mode
+    return d;
+}
+
+// Shared-memory matrix descriptor of a K-major operand without swizzle: core matrices of
+// 8 rows x 16 bytes stored contiguously (rows 16 B apart); the core matrix next along K
+// sits `lbo` bytes further, the next group of 8 rows `sbo` bytes further. Any 16-byte
+// aligned start address is valid, so a view shifted by whole rows is a plain offset.
+__device__ __forceinline__ uint64_t smem_desc_noswz(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;                       // descriptor version (sm_100); layout 0 = no swizzle
     return d;
 }
 

@@ -1,22 +1,26 @@
 """Time-to-relMSE of the learned denoiser against plain accumulation.
 
-The scene is the Cornell box (256-spp-class workload of kuafu's example, built
-procedurally) rendered at 1920x1080, path depth 5, no Russian roulette. The
-experiment, all on one GPU:
+The scene is the Cornell box (kuafu's example scene, built procedurally) rendered
+at 1920x1080, path depth 5, no Russian roulette. The experiment, all on one GPU:
 
 1. Reference: two independent FP64 accumulations (seeds A and B) of ref_spp / 2
    samples each; ref = their mean. relMSE(A, B) / 4 estimates the reference's own
    noise floor (the expected relMSE of a noise-free image against this reference),
-   reported as `ref_floor`. "Debiased" relMSE values subtract that floor.
-2. Plain accumulation (an independent seed): frames of `plain_frame_spp` samples,
-   relMSE after each checkpoint, cumulative GPU time from CUDA events.
+   reported as `ref_floor`; the default 40960 spp put it near 4.6e-4, well below
+   the 1e-3 target, so raw relMSE against the reference can be measured down to it.
+2. Plain accumulation (an independent seed) into the FP64 sum: frames of
+   `plain_frame_spp` samples, checkpoints at powers of two to 1024 spp and every
+   `plain_checkpoint_step` samples after that, until the raw relMSE reaches the
+   smallest threshold (or `plain_max_spp`); cumulative GPU time of the frames
+   from CUDA events (the checkpoints' relMSE evaluations are not counted).
 3. Learned denoiser: trained on this renderer's own pairs (Cornell variations at
-   256x256, inputs at 1..64 spp, targets at high spp), then applied to single
-   frames of k spp of the held-out scene; time = render + denoise (CUDA events).
-4. For each threshold tau: the time plain accumulation needs to reach relMSE <= tau
-   (measured, or extrapolated from its c / N fit past the last checkpoint, flagged)
-   and the time the denoised form needs (smallest k whose denoised frame reaches
-   tau, or None).
+   256x256, inputs cycling 1..1024 spp, targets at 4096 spp), then applied to
+   single frames of k spp of the held-out scene; time = render + denoise (CUDA
+   events).
+4. For each threshold tau: the measured time plain accumulation needs to reach raw
+   relMSE <= tau and the time the denoised form needs (smallest k whose denoised
+   frame reaches tau), and their ratio. "Debiased" values (raw minus ref_floor)
+   are reported beside them.
 
 relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2), reduced
 in FP64 on the GPU (kf_relmse).
@@ -105,10 +109,11 @@ def _accumulate(r, cfg, cam, seed, spp_total, frame_spp):
     return _fp64_mean(r, cam)
 
 
-def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp=8, plain_max_spp=1024,
-        train_views=66, train_size=256, train_high_spp=64, train_high_frames=64, train_iters=4000,
-        train_batch=8, train_crop=128, lr=1e-3, denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024),
-        thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3), depth=5, log=print) -> dict:
+def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_spp=8, plain_checkpoint_step=2048,
+        plain_max_spp=65536, train_views=66, train_size=256, train_high_spp=64,
+        train_high_frames=64, train_iters=4000, train_batch=8, train_crop=128, lr=1e-3,
+        denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3),
+        depth=5, log=print) -> dict:
     cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
     res = {"scene": "cornell", "width": width, "height": height, "depth": depth, "eps": EPS}
     with api.Kuafu(cfg) as r:
@@ -123,15 +128,17 @@ def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp
         res["reference"] = {"spp": ref_spp, "accumulation": "fp64", "halves_relmse": 4.0 * floor,
                             "ref_floor": floor, "seconds": time.perf_counter() - t0}
         log(f"reference {ref_spp} spp: floor {floor:.4e} ({time.perf_counter() - t0:.1f} s)")
+        del a, b
 
-        # 2. plain accumulation
+        # 2. plain accumulation (FP64 sum of equal frames), measured until the smallest
+        #    threshold is reached
         timer = _Timer(r)
+        tau_min = min(thresholds)
         cfg.setSeed(7)
         cfg.setPerPixelSampleRate(plain_frame_spp)
         cfg.setAccumulatingFrames(True)
         r.applyConfig()
-        r.resetFrame()
-        r.run()  # graph capture outside the timed frames
+        r.run()  # graph capture outside the timed frames; the reset below discards this frame
         r.synchronize()
         r.resetFrame()
         plain = []
@@ -143,17 +150,17 @@ def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp
             t_ms += timer.ms
             spp += plain_frame_spp
             if spp >= next_cp:
-                img = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
-                e = _gpu_relmse(r, img, ref)
+                e = _gpu_relmse(r, _fp64_mean(r, cam), ref)
                 plain.append({"spp": spp, "ms": t_ms, "relmse": e, "relmse_debiased": e - floor})
-                next_cp *= 2
+                next_cp = next_cp * 2 if next_cp < 1024 else next_cp + plain_checkpoint_step
+                if e <= tau_min:
+                    break
+        s64 = r.downloadAov(cam, N.KF_AOV_SUM_F64)
         res["plain"] = plain
+        res["plain_check"] = {"frames_in_fp64_sum": float(s64[..., 3].max()), "spp": spp}
         log("plain: " + ", ".join(f"{p['spp']}spp {p['relmse']:.3e}" for p in plain))
-        # c / N fit on the debiased values of the last half of the checkpoints
-        tail = [p for p in plain if p["spp"] >= plain[len(plain) // 2]["spp"]]
-        c_fit = float(np.median([max(p["relmse_debiased"], 0.0) * p["spp"] for p in tail]))
         ms_per_spp = plain[-1]["ms"] / plain[-1]["spp"]
-        res["plain_fit"] = {"c": c_fit, "ms_per_spp": ms_per_spp}
+        res["plain_fit"] = {"ms_per_spp": ms_per_spp}
 
         # 3. denoiser training on Cornell variations
         d = api.Denoiser(r, seed=0)
@@ -214,28 +221,29 @@ def run(width=1920, height=1080, ref_spp=4096, ref_frame_spp=64, plain_frame_spp
         res["denoiser_flops_per_frame"] = flops
         d.close()
 
-    # 5. time to each threshold
+    # 5. time to each threshold: measured on both arms, raw relMSE (debiased beside it)
     ttr = []
     for tau in thresholds:
         row = {"tau": tau}
         for key in ("relmse", "relmse_debiased"):
             hit = next((p for p in plain if p[key] <= tau), None)
-            if hit is not None:
-                pt, how = hit["ms"], "measured"
-            elif key == "relmse_debiased" and c_fit > 0:
-                pt, how = c_fit / tau * ms_per_spp, "extrapolated c/N"
-            else:
-                pt, how = None, "not reached"
+            pt, how = (hit["ms"], "measured") if hit is not None else (None, "not reached")
             dh = [p for p in den if p[key] <= tau]
             dt = min(p["ms"] for p in dh) if dh else None
-            row[key] = {"plain_ms": pt, "plain": how, "denoised_ms": dt,
-                        "speedup": (pt / dt) if (pt and dt) else None}
+            dk = min((p for p in dh), key=lambda p: p["ms"])["spp"] if dh else None
+            row[key] = {"plain_ms": pt, "plain": how, "plain_spp": hit["spp"] if hit else None, "denoised_ms": dt,
+                        "denoised_input_spp": dk, "speedup": (pt / dt) if (pt and dt) else None}
         ttr.append(row)
     res["time_to_relmse"] = ttr
+    floor_4096 = floor * ref_spp / 4096.0  # the floor falls as 1 / spp
+    res["note_4096spp_reference"] = (
+        f"against a 4096-spp reference the floor would be about {floor_4096:.2e} (the relMSE of an independent "
+        f"estimate includes the reference's own noise), so nothing could be measured below 1e-3 against it; the "
+        f"reference here has {ref_spp} spp")
     return res
 
 
-SMALL = dict(width=480, height=272, ref_spp=1024, plain_max_spp=256, train_views=18, train_iters=300,
+SMALL = dict(width=480, height=272, ref_spp=4096, plain_max_spp=8192, plain_checkpoint_step=512, train_views=18, train_iters=300,
              train_crop=96, train_high_frames=16)
 
 
