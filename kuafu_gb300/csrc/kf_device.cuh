@@ -320,6 +320,10 @@ KF_DEV bool intersect_tri(const PRay& r, float4 a, float4 b, float4 c, float tmi
 // widened by 1 + 2*gamma(3) (Ize, JCGT 2013) so no box is culled by rounding.
 // Returns a 4-bit mask of children hit and their entry distances.
 #define KF_BOX_WIDEN (1.0f + 2.0f * (3.0f * 0x1.0p-24f) / (1.0f - 3.0f * 0x1.0p-24f))
+// The current closest hit is widened too before a box is culled against it: a triangle
+// whose computed t ties the closest hit (two walls meeting at a corner) may sit in a box
+// whose computed entry distance lies a few ulp beyond that t; the tie rule needs it tested.
+#define KF_TMAX_WIDEN (1.0f + 0x1.0p-19f)
 
 KF_DEV float lane(float4 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w)); }
 KF_DEV int lanei(int4 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w)); }
@@ -348,7 +352,7 @@ KF_DEV int box4(const PRay& r, const Node4& n, float tmin, float tmax, float tn_
         tn = fmaxf(tn, t0z);
         tf = fminf(tf, t1z);
         tn_out[c] = tn;
-        if (tn <= fminf(tf * KF_BOX_WIDEN, tmax)) mask |= 1 << c;
+        if (tn <= fminf(tf * KF_BOX_WIDEN, tmax * KF_TMAX_WIDEN)) mask |= 1 << c;
     }
     return mask;
 }

@@ -68,6 +68,33 @@ __global__ void k_rebase(const Node4* __restrict__ in, uint32_t n, uint32_t node
     out[i] = o;
 }
 
+// k_tri_gather over every geometry at once: out[j] for j in the triangle pool, the
+// geometry found by binary search over the pool offsets of the `ng` geometries
+// (geom[g] = {vertex offset, triangle offset, triangles, flags}); order holds each
+// geometry's leaf order (geometry-local primitive ids) at its triangle offset.
+__global__ void k_tri_gather_all(const float4* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                 const uint32_t* __restrict__ order, const uint4* __restrict__ geom, uint32_t ng,
+                                 uint32_t n, Tri* out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t lo = 0, hi = ng;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (geom[mid].y <= j) lo = mid;
+        else hi = mid;
+    }
+    const uint4 g = geom[lo];
+    if (j - g.y >= g.z) return; // not a triangle of any geometry (cannot happen: the pool is dense)
+    const uint32_t prim = order[j];
+    float4 p[3];
+    for (int k = 0; k < 3; ++k) p[k] = verts[3 * (size_t)(g.x + idx[3 * (size_t)(g.y + prim) + k])];
+    Tri t;
+    t.v0 = make_float4(p[0].x, p[0].y, p[0].z, __uint_as_float(prim));
+    t.v1 = make_float4(p[1].x, p[1].y, p[1].z, 0.0f);
+    t.v2 = make_float4(p[2].x, p[2].y, p[2].z, 0.0f);
+    out[j] = t;
+}
+
 __global__ void k_map_ids(const uint32_t* __restrict__ order, const uint32_t* __restrict__ ids, uint32_t n,
                           uint32_t* out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -265,7 +292,39 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             work();
             for (std::thread& t : pool) t.join();
         }
-        for (size_t gi = 0; gi < ng; ++gi) {
+        if (sah) {
+            // every BLAS in one pool upload: children rebased on the host (inner links by the
+            // BLAS's first node, leaf links by its first triangle), one leaf-order array at the
+            // triangle offsets, one gather kernel for the whole triangle pool; no per-BLAS sync
+            std::vector<Node4> pool;
+            pool.reserve(total_nodes_est);
+            std::vector<uint32_t> order_all(std::max<size_t>(nt, 1), 0u);
+            for (size_t gi = 0; gi < ng; ++gi) {
+                if (geom[gi].z == 0) continue;
+                G.blas_root[gi] = (uint32_t)pool.size();
+                root_box(sah_nodes[gi][0], G.blas_box[gi]);
+                const uint32_t nb = (uint32_t)pool.size(), tb = geom[gi].y;
+                for (Node4 nd : sah_nodes[gi]) {
+                    int* c = &nd.child.x;
+                    const int* k = &nd.cnt.x;
+                    for (int q = 0; q < 4; ++q) {
+                        if (k[q] == 0) c[q] += (int)nb;
+                        else if (k[q] > 0) c[q] += (int)tb;
+                    }
+                    pool.push_back(nd);
+                }
+                std::copy(sah_order[gi].begin(), sah_order[gi].end(), order_all.begin() + tb);
+            }
+            if (!pool.empty()) G.blas_nodes.upload(pool.data(), pool.size(), st);
+            order.upload(order_all.data(), order_all.size(), st);
+            if (nt > 0) {
+                k_tri_gather_all<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(
+                    G.verts.ptr, G.indices.ptr, order.ptr, G.geom.ptr, (uint32_t)ng, (uint32_t)nt, G.tris.ptr);
+                KF_CUDA_CHECK(cudaGetLastError());
+            }
+            node_base = (uint32_t)pool.size();
+        }
+        for (size_t gi = 0; gi < ng && !sah; ++gi) {
             const uint32_t ntri = geom[gi].z;
             if (ntri == 0) continue;
             int nn;

@@ -131,7 +131,7 @@ __device__ __forceinline__ int box4_dir(const PRay& r, const float4* p, float tm
         tn = fmaxf(tn, t0z);
         tf = fminf(tf, t1z);
         tn_out[c] = tn;
-        if (tn <= fminf(tf * KF_BOX_WIDEN, tmax)) mask |= 1 << c;
+        if (tn <= fminf(tf * KF_BOX_WIDEN, tmax * KF_TMAX_WIDEN)) mask |= 1 << c;
     }
     return mask;
 }

@@ -326,6 +326,9 @@ inline bool intersect_tri(const Ray32& r, const float* v0, const float* v1, cons
 // Conservative slab test: far distances widened by 1 + 2*gamma(3) (Ize,
 // "Robust BVH Ray Traversal", JCGT 2(2), 2013).
 constexpr float kBoxWiden = 1.0f + 2.0f * (3.0f * 0x1.0p-24f) / (1.0f - 3.0f * 0x1.0p-24f);
+// the closest hit so far is widened as well, so a box holding a triangle whose t ties it
+// (rounded entry distance a few ulp beyond) is still opened and the tie rule decides
+constexpr float kTmaxWiden = 1.0f + 0x1.0p-19f;
 inline bool box_hit(const Ray32& r, const float* lo, const float* hi, float tmin, float tmax) {
     float tn = tmin, tf = INFINITY;
     for (int a = 0; a < 3; ++a) {
@@ -336,7 +339,7 @@ inline bool box_hit(const Ray32& r, const float* lo, const float* hi, float tmin
         tn = std::fmax(tn, t0);
         tf = std::fmin(tf, t1);
     }
-    return tn <= std::fmin(tf * kBoxWiden, tmax);
+    return tn <= std::fmin(tf * kBoxWiden, tmax * kTmaxWiden);
 }
 
 struct BvhNode {
