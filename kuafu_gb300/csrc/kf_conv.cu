@@ -229,14 +229,18 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 // A tile is R output rows x 128 pixels x n_tile output channels: R accumulators of
 // n_tile TMEM columns, double-buffered so the epilogue of one tile overlaps the MMAs of
 // the next. Per chunk of CK input channels one 5D TMA box brings the tile's input halo,
-// (R + 2) rows x 130 pixels, into shared memory as [row][channel group][pixel][8
-// channels]: a K-major operand without swizzle (8 pixels x 16 bytes per core matrix,
-// core matrices 128 bytes apart along M and 130 x 16 bytes apart along K). The A
-// operand of tap (dy, dx) for output row r is that buffer viewed from row r + dy + 1,
-// pixel dx + 1 on: a descriptor offset, so the halo is read from L2 once per chunk
-// and used by all 9 taps (the per-tap kernel above reads 9 shifted boxes). The
-// weights of a chunk ([tap][n_tile][CK], swizzled rows of CK channels) stream with the
-// halo, or, when one chunk covers all input channels, are loaded once per CTA.
+// (R + 2) rows x 130 pixels, into shared memory as [row][channel group][pixel][8 channels]: a
+// K-major operand without swizzle (8 pixels x 16 bytes per core matrix, core matrices
+// 128 bytes apart along M and 130 x 16 bytes apart along K). The A operand of tap
+// (dy, dx) for output row r is that buffer viewed from row r + dy + 1, pixel dx + 1 on:
+// a descriptor offset, so the halo is read from L2 once per chunk and used by all 9
+// taps (the per-tap kernel above reads 9 shifted boxes). The weights of a chunk
+// ([tap][n_tile][CK], swizzled rows of CK channels) stream with the halo by TMA, or,
+// when one chunk covers all input channels, are loaded once per CTA.
+//
+// The epilogue can also do the 2x2 average pooling that follows some layers (rows are
+// paired inside a tile, the right neighbour is the next lane), saving the pass that
+// would read the layer's output again.
 //
 // Warp 0 lane 0: TMA producer (kHaloStages-deep ring). Warp 1 lane 0: MMA issuer.
 // Warps 2-5: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels.
@@ -262,6 +266,7 @@ struct HaloParams {
     __nv_bfloat16* out;
     int out_cstride, out_coff;
     float* outf;
+    __nv_bfloat16* pool_out;   // fused 2x2 average pooling into a dense [N][H/2][W/2][Cout] tensor, or null
 };
 
 template <int CK>
@@ -414,39 +419,81 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
             int n_img, y0, x0;
             tile_origin(t, n_img, y0, x0);
             const int px = x0 + px_in_tile;
-            for (int r = 0; r < p.R; ++r) {
-                const int py = y0 + r;
-                const bool valid = px < p.W && py < p.H;
+            // one output row's 8 channels [cc, cc + 8) of this pixel (BF16 or FP32)
+            auto emit8 = [&](const float(&v)[8], int py, int cc) {
+                const int co = n0 + cc;
+                if (!(px < p.W && py < p.H) || co >= p.Cout) return;
                 const size_t base = ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
-                const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
-                for (int c = 0; c < p.n_tile; c += 16) {
-                    uint32_t r0[8], r1[8];
-                    tc::tmem_ld8(tmem + ((uint32_t)(lg * 32) << 16) + col0 + (uint32_t)c, r0);
-                    tc::tmem_ld8(tmem + ((uint32_t)(lg * 32) << 16) + col0 + (uint32_t)(c + 8), r1);
-                    tc::tmem_ld_wait();
+                if (p.outf) {
+                    for (int q = 0; q < 8 && co + q < p.Cout; ++q) p.outf[base + co + q] = v[q];
+                    return;
+                }
+                __nv_bfloat162 q2[4];
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const uint32_t* rr = h ? r1 : r0;
-                        const int cc = c + 8 * h, co = n0 + cc;
-                        if (!valid || co >= p.Cout) continue;
-                        float v[8];
+                for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                const uint4 packed = *reinterpret_cast<const uint4*>(q2);
+                __nv_bfloat16* dst = p.out + base + co;
+                if (co + 8 <= p.Cout && ((p.out_coff + co) & 7) == 0 && (p.out_cstride & 7) == 0)
+                    *reinterpret_cast<uint4*>(dst) = packed;
+                else
+                    for (int q = 0; q < 8 && co + q < p.Cout; ++q) dst[q] = __float2bfloat16_rn(v[q]);
+            };
+            auto act = [&](uint32_t raw, int cc) {
+                const float v = __uint_as_float(raw) + sbias[cc];
+                return p.relu ? fmaxf(v, 0.0f) : v;
+            };
+            const uint32_t lanes = (uint32_t)(lg * 32) << 16;
+            if (!p.pool_out) {
+                for (int r = 0; r < p.R; ++r) {
+                    const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
+                    for (int c = 0; c < p.n_tile; c += 16) { // two TMEM loads per wait
+                        uint32_t r0[8], r1[8];
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, r0);
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(c + 8), r1);
+                        tc::tmem_ld_wait();
+                        float v0[8], v1[8];
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
-                            v[q] = __uint_as_float(rr[q]) + sbias[cc + q];
-                            if (p.relu) v[q] = fmaxf(v[q], 0.0f);
+                            v0[q] = act(r0[q], c + q);
+                            v1[q] = act(r1[q], c + 8 + q);
                         }
-                        if (p.outf) {
-                            for (int q = 0; q < 8 && co + q < p.Cout; ++q) p.outf[base + co + q] = v[q];
-                            continue;
+                        emit8(v0, y0 + r, c);
+                        emit8(v1, y0 + r, c + 8);
+                    }
+                }
+            } else {
+                // rows in pairs (R and y0 are even): the 2x2 average of the BF16 outputs, as the
+                // separate pooling pass computes it ((a + b) + c) + d over (2y, 2x), (2y, 2x+1),
+                // (2y+1, 2x), (2y+1, 2x+1); the right neighbour is the next lane
+                const int Hh = p.H / 2, Wh = p.W / 2;
+                for (int r = 0; r < p.R; r += 2) {
+                    const int py = y0 + r;
+                    const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
+                    for (int c = 0; c < p.n_tile; c += 8) {
+                        uint32_t ra[8], rc[8];
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, ra);
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(p.n_tile + c), rc);
+                        tc::tmem_ld_wait();
+                        float va[8], vc[8], pooled[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            va[q] = act(ra[q], c + q);
+                            vc[q] = act(rc[q], c + q);
+                            const float a = __bfloat162float(__float2bfloat16_rn(va[q]));
+                            const float cv = __bfloat162float(__float2bfloat16_rn(vc[q]));
+                            const float bv = __shfl_xor_sync(0xFFFFFFFFu, a, 1);
+                            const float dv = __shfl_xor_sync(0xFFFFFFFFu, cv, 1);
+                            pooled[q] = 0.25f * (((a + bv) + cv) + dv);
                         }
-                        __nv_bfloat16* dst = p.out + base + co;
-                        if (co + 8 <= p.Cout && ((p.out_coff + co) & 7) == 0 && (p.out_cstride & 7) == 0) {
+                        emit8(va, py, c);
+                        emit8(vc, py + 1, c);
+                        const int co = n0 + c;
+                        if ((lane & 1) == 0 && px + 1 < p.W && py + 1 < p.H && co < p.Cout) {
                             __nv_bfloat162 q2[4];
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
-                            *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(q2);
-                        } else {
-                            for (int q = 0; q < 8 && co + q < p.Cout; ++q) dst[q] = __float2bfloat16_rn(v[q]);
+                            for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(pooled[2 * q], pooled[2 * q + 1]);
+                            const size_t pb = ((size_t)((size_t)n_img * Hh + py / 2) * Wh + px / 2) * p.Cout + co;
+                            *reinterpret_cast<uint4*>(p.pool_out + pb) = *reinterpret_cast<const uint4*>(q2);
                         }
                     }
                 }
@@ -575,13 +622,14 @@ template <int CK> void launch_halo(dim3 grid, const CUtensorMap& x, const CUtens
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
-// The halo kernel for images at least one 128-pixel tile wide; false when no shape fits.
-bool conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
-                  const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
-                  cudaStream_t st, float* y_f32) {
+// The halo kernel for images at least one 128-pixel tile wide. Returns 0 when no shape
+// fits (the caller takes the per-tile kernel), 1 when it ran, 2 when it also did the fused work.
+int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
+                 const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
+                 cudaStream_t st, float* y_f32, const ConvFuse* fuse) {
     const int n_tile = Cout_rows <= 256 ? Cout_rows : 128;
     HaloShape h;
-    if (W < 128 || !halo_shape(Cin, n_tile, h)) return false;
+    if (W < 128 || !halo_shape(Cin, n_tile, h)) return 0;
     // input as [n][y][channel group][x][8 channels]: dims (8, W, Cin / 8, H, N)
     const uint64_t xdims[5] = {8, (uint64_t)W, (uint64_t)Cin / 8, (uint64_t)H, (uint64_t)N};
     const uint64_t xstr[4] = {(uint64_t)Cin * 2, 16, (uint64_t)W * Cin * 2, (uint64_t)H * W * Cin * 2};
@@ -612,6 +660,13 @@ bool conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     p.outf = y_f32;
     p.out_cstride = y_cstride;
     p.out_coff = y_coff;
+    bool fused = false;
+    // pooling pairs rows inside a tile (R even) and reads the right neighbour's lane
+    if (fuse && fuse->pool_out && y && !y_f32 && Cout % 8 == 0 && n_tile % 8 == 0 && h.R % 2 == 0 && H % 2 == 0 &&
+        W % 2 == 0) {
+        p.pool_out = fuse->pool_out;
+        fused = true;
+    }
     const int slices = (Cout_rows + n_tile - 1) / n_tile;
     const int per_slice = std::max(1, num_sms() / slices);
     const dim3 grid((unsigned)std::min(p.num_tiles, per_slice), (unsigned)slices, 1);
@@ -619,14 +674,14 @@ bool conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
         launch_halo<32>(grid, mx, mw, p, h.smem, st);
     else
         launch_halo<16>(grid, mx, mw, p, h.smem, st);
-    return true;
+    return fused ? 2 : 1;
 }
 
 } // namespace
 
-void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
+bool conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
                   const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
-                  cudaStream_t st, float* y_f32) {
+                  cudaStream_t st, float* y_f32, const ConvFuse* fuse) {
     KF_REQUIRE(N > 0 && H > 0 && W > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: empty tensor");
     KF_REQUIRE(y || y_f32, KF_ERR_INVALID_ARGUMENT, "conv3x3: no output tensor");
     KF_REQUIRE(Cin % 32 == 0 && Cin > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: input channels must be a multiple of 32");
@@ -635,7 +690,9 @@ void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     KF_REQUIRE(y_coff >= 0 && y_coff + Cout <= y_cstride, KF_ERR_INVALID_ARGUMENT, "conv3x3: output slice");
     KF_REQUIRE(((uintptr_t)x & 15) == 0 && ((uintptr_t)w & 15) == 0, KF_ERR_INVALID_ARGUMENT,
                "conv3x3: tensors must be 16-byte aligned");
-    if (conv3x3_halo(x, N, H, W, Cin, w, Cout_rows, bias, Cout, relu, y, y_cstride, y_coff, st, y_f32)) return;
+    const int halo = conv3x3_halo(x, N, H, W, Cin, w, Cout_rows, bias, Cout, relu, y, y_cstride, y_coff, st, y_f32,
+                                  fuse);
+    if (halo) return halo == 2;
     // narrow images: one CTA per tile of bw x bh = 128 pixels, 9 tap-shifted boxes per chunk
     int bw = 128;
     while (bw > W && bw > 8) bw >>= 1;
@@ -672,6 +729,7 @@ void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
         launch_tc<0, 64, 2>(grid, ma, mb, p, st);
     else
         launch_tc<0, 64, 3>(grid, ma, mb, p, st);
+    return false;
 }
 
 void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, int K, float* d, int ldd, int splits,

@@ -8,13 +8,22 @@
 
 namespace kf {
 
+// Work a convolution can take over from the pass that follows it: 2x2 average pooling of
+// its BF16 output into a dense [N][H/2][W/2][Cout] tensor. The values equal those of the
+// separate pass (both read the BF16-rounded outputs).
+struct ConvFuse {
+    __nv_bfloat16* pool_out = nullptr;
+};
+
 // y[n, y, x, y_coff + co] = act(bias[co] + sum_{tap, ci} x[n, y+dy, x+dx, ci] * w[tap][co][ci])
 // NHWC BF16, zero padding, FP32 accumulation on tcgen05. w is [9][Cout_rows][Cin] with
 // Cout_rows a multiple of 16 (rows >= Cout are computed and dropped); Cin % 32 == 0.
 // With y_f32 set, the output is written there in FP32 (same strides) and y is unused.
-void conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
+// Returns true when it also did the fused work asked for in `fuse` (the persistent halo
+// kernel does it for suitable shapes; otherwise the caller runs the separate pass).
+bool conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
                   const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
-                  cudaStream_t st, float* y_f32 = nullptr);
+                  cudaStream_t st, float* y_f32 = nullptr, const ConvFuse* fuse = nullptr);
 
 // d[m][n] += sum_k a[m][k] * b[n][k]   (BF16 K-major operands, FP32 atomics; split-K over `splits`)
 void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, int K, float* d, int ldd, int splits,

@@ -365,6 +365,15 @@ __global__ void k_loss(const float* __restrict__ pred, const float4* __restrict_
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc * inv);
 }
 
+// A training target from the FP64 accumulation: sum of the frames' pixel means / frames.
+__global__ void k_target_from_sum64(const dbl4* __restrict__ sum, size_t n, float4* out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const dbl4 v = sum[i];
+        const double inv = v.w > 0.0 ? 1.0 / v.w : 0.0;
+        out[i] = make_float4((float)(v.x * inv), (float)(v.y * inv), (float)(v.z * inv), 1.0f);
+    }
+}
+
 // crop gather: features [n][H][W][32], residual bases and targets -> batch [b][c][c]
 __global__ void k_gather_crops(const bf16* __restrict__ feat, const float4* __restrict__ base,
                                const float4* __restrict__ tgt, int H, int W, const int4* __restrict__ crops, int B,
@@ -573,10 +582,12 @@ struct Ctx {
     size_t P(int level) const { return (size_t)n * H(level) * W(level); }
 };
 
-void conv_fwd(Ctx& c, int li, int level, TRef x, TRef y) {
+// The convolution, and (when `fuse` is given) the pooling / upsampling pass after it: the
+// persistent conv kernel does that work in its epilogue where it can, else the pass runs here.
+bool conv_fwd(Ctx& c, int li, int level, TRef x, TRef y, const ConvFuse* fuse = nullptr) {
     const Layer& l = c.d.L[li];
-    conv3x3_bf16(x.p, c.n, c.H(level), c.W(level), x.cs, c.d.wf.ptr + l.wf_off, l.rows, c.d.params.ptr + l.b_off,
-                 l.cout, l.relu, y.p, y.cs, y.co, c.st);
+    return conv3x3_bf16(x.p, c.n, c.H(level), c.W(level), x.cs, c.d.wf.ptr + l.wf_off, l.rows,
+                        c.d.params.ptr + l.b_off, l.cout, l.relu, y.p, y.cs, y.co, c.st, nullptr, fuse);
 }
 
 // Backward of y = act(conv(x) + b): accumulates dW, db; writes gx (if gx.p) = dL/dx.
@@ -621,34 +632,39 @@ void up_fwd(Ctx& c, TRef x, int level_hi, TRef y) {
     const size_t n = c.P(level_hi + 1) * x.c / 8;
     k_up_fwd<<<grid_for(n), 256, 0, c.st>>>(x.p, x.c, c.n, c.H(level_hi), c.W(level_hi), y.p, y.cs, y.co);
 }
+// conv into y, then 2x2 pooling of y into `pooled` (at level + 1)
+void conv_pool(Ctx& c, int li, int level, TRef x, TRef y, TRef pooled) {
+    ConvFuse f;
+    f.pool_out = pooled.p;
+    if (!conv_fwd(c, li, level, x, y, &f)) pool_fwd(c, y, level, pooled);
+}
+// conv into y, then nearest 2x upsampling of y into the channel slice `up` (at level - 1).
+// A separate pass: written from the conv epilogue the four scattered copies per pixel cost
+// more than reading the output once more.
+void conv_up(Ctx& c, int li, int level, TRef x, TRef y, TRef up) {
+    conv_fwd(c, li, level, x, y);
+    up_fwd(c, y, level - 1, up);
+}
 
 // prediction (in a.head) = network(T_IN) + base (FP32 residual, optional)
 void forward(Ctx& c, const float4* base) {
     Acts& a = c.d.acts;
     conv_fwd(c, 0, 0, T(a, T_IN), T(a, T_E0A));
-    conv_fwd(c, 1, 0, T(a, T_E0A), S(a, T_CAT0, 64, 32));
-    pool_fwd(c, S(a, T_CAT0, 64, 32), 0, T(a, T_P0));
+    conv_pool(c, 1, 0, T(a, T_E0A), S(a, T_CAT0, 64, 32), T(a, T_P0));
     conv_fwd(c, 2, 1, T(a, T_P0), T(a, T_E1A));
-    conv_fwd(c, 3, 1, T(a, T_E1A), S(a, T_CAT1, 96, 64));
-    pool_fwd(c, S(a, T_CAT1, 96, 64), 1, T(a, T_P1));
+    conv_pool(c, 3, 1, T(a, T_E1A), S(a, T_CAT1, 96, 64), T(a, T_P1));
     conv_fwd(c, 4, 2, T(a, T_P1), T(a, T_E2A));
-    conv_fwd(c, 5, 2, T(a, T_E2A), S(a, T_CAT2, 128, 96));
-    pool_fwd(c, S(a, T_CAT2, 128, 96), 2, T(a, T_P2));
+    conv_pool(c, 5, 2, T(a, T_E2A), S(a, T_CAT2, 128, 96), T(a, T_P2));
     conv_fwd(c, 6, 3, T(a, T_P2), T(a, T_E3A));
-    conv_fwd(c, 7, 3, T(a, T_E3A), S(a, T_CAT3, 160, 128));
-    pool_fwd(c, S(a, T_CAT3, 160, 128), 3, T(a, T_P3));
+    conv_pool(c, 7, 3, T(a, T_E3A), S(a, T_CAT3, 160, 128), T(a, T_P3));
     conv_fwd(c, 8, 4, T(a, T_P3), T(a, T_E4A));
-    conv_fwd(c, 9, 4, T(a, T_E4A), T(a, T_E4B));
-    up_fwd(c, T(a, T_E4B), 3, S(a, T_CAT3, 0, 160));
+    conv_up(c, 9, 4, T(a, T_E4A), T(a, T_E4B), S(a, T_CAT3, 0, 160));
     conv_fwd(c, 10, 3, T(a, T_CAT3), T(a, T_D3A));
-    conv_fwd(c, 11, 3, T(a, T_D3A), T(a, T_D3B));
-    up_fwd(c, T(a, T_D3B), 2, S(a, T_CAT2, 0, 128));
+    conv_up(c, 11, 3, T(a, T_D3A), T(a, T_D3B), S(a, T_CAT2, 0, 128));
     conv_fwd(c, 12, 2, T(a, T_CAT2), T(a, T_D2A));
-    conv_fwd(c, 13, 2, T(a, T_D2A), T(a, T_D2B));
-    up_fwd(c, T(a, T_D2B), 1, S(a, T_CAT1, 0, 96));
+    conv_up(c, 13, 2, T(a, T_D2A), T(a, T_D2B), S(a, T_CAT1, 0, 96));
     conv_fwd(c, 14, 1, T(a, T_CAT1), T(a, T_D1A));
-    conv_fwd(c, 15, 1, T(a, T_D1A), T(a, T_D1B));
-    up_fwd(c, T(a, T_D1B), 0, S(a, T_CAT0, 0, 64));
+    conv_up(c, 15, 1, T(a, T_D1A), T(a, T_D1B), S(a, T_CAT0, 0, 64));
     conv_fwd(c, 16, 0, T(a, T_CAT0), T(a, T_D0A));
     conv_fwd(c, 17, 0, T(a, T_D0A), T(a, T_D0B));
     {
@@ -832,10 +848,11 @@ void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint3
     r->frame_count = -1;
     render_frame(r, s, c, low_spp);
     camera_features(c, low_spp, d->ds_feat.ptr + npix * 32 * k, d->ds_base.ptr + npix * k, c->height, c->width, st);
-    // target: running mean of high_frames frames of high_spp samples
+    // target: high_frames frames of high_spp samples, averaged from the FP64 accumulation
     r->frame_count = -1;
     for (uint32_t f = 0; f < high_frames; ++f) render_frame(r, s, c, high_spp);
-    KF_CUDA_CHECK(cudaMemcpyAsync(d->ds_tgt.ptr + npix * k, c->accum.ptr, npix * 16, cudaMemcpyDeviceToDevice, st));
+    k_target_from_sum64<<<grid_for(npix), 256, 0, st>>>(c->sum64.ptr, npix, d->ds_tgt.ptr + npix * k);
+    KF_CUDA_CHECK(cudaGetLastError());
     KF_CUDA_CHECK(cudaStreamSynchronize(st));
     ++d->ds_n;
 }

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 
 #include "kf_bvh.h"
 #include "kf_host.h"
@@ -265,12 +266,49 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         const bool sah = r->cfg.bvh_builder == 1;
         std::vector<std::vector<Node4>> sah_nodes(sah ? ng : 0);
         std::vector<std::vector<uint32_t>> sah_order(sah ? ng : 0);
+        // geometries whose triangles are byte-identical (same positions and indices, the
+        // materials may differ) share one build; each still gets its own copy of the nodes
+        // and triangles, so the traversal is the same as with separate builds
+        std::vector<size_t> build_of(ng);
+        std::vector<size_t> to_build;
+        if (sah) {
+            std::unordered_map<uint64_t, std::vector<size_t>> seen;
+            auto fnv = [](uint64_t h, const void* p, size_t n) {
+                const unsigned char* b = static_cast<const unsigned char*>(p);
+                for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
+                return h;
+            };
+            auto same = [&](const kf_geometry_s* a, const kf_geometry_s* b) {
+                if (a->indices.size() != b->indices.size() || a->vertices.size() != b->vertices.size()) return false;
+                if (std::memcmp(a->indices.data(), b->indices.data(), a->indices.size() * sizeof(uint32_t))) return false;
+                for (size_t v = 0; v < a->vertices.size(); ++v)
+                    if (std::memcmp(a->vertices[v].pos, b->vertices[v].pos, sizeof(float) * 3)) return false;
+                return true;
+            };
+            for (size_t gi = 0; gi < ng; ++gi) {
+                const kf_geometry_s* g = s->geometries[gi];
+                uint64_t h = fnv(0xcbf29ce484222325ull, g->indices.data(), g->indices.size() * sizeof(uint32_t));
+                for (const kf_vertex& v : g->vertices) h = fnv(h, v.pos, sizeof(float) * 3);
+                std::vector<size_t>& cand = seen[h];
+                size_t found = SIZE_MAX;
+                for (size_t c : cand)
+                    if (same(s->geometries[c], g)) found = c;
+                if (found == SIZE_MAX) {
+                    cand.push_back(gi);
+                    to_build.push_back(gi);
+                    build_of[gi] = gi;
+                } else {
+                    build_of[gi] = found;
+                }
+            }
+        }
         if (sah) {
             const int leaf = (int)std::max(1u, r->cfg.blas_leaf_size);
             std::atomic<size_t> next{0};
             auto work = [&]() {
                 std::vector<float> blo, bhi;
-                for (size_t gi; (gi = next.fetch_add(1)) < ng;) {
+                for (size_t k; (k = next.fetch_add(1)) < to_build.size();) {
+                    const size_t gi = to_build[k];
                     const kf_geometry_s* g = s->geometries[gi];
                     const size_t nt_g = g->indices.size() / 3;
                     blo.resize(3 * nt_g);
@@ -301,10 +339,11 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             std::vector<uint32_t> order_all(std::max<size_t>(nt, 1), 0u);
             for (size_t gi = 0; gi < ng; ++gi) {
                 if (geom[gi].z == 0) continue;
+                const size_t bi = build_of[gi];
                 G.blas_root[gi] = (uint32_t)pool.size();
-                root_box(sah_nodes[gi][0], G.blas_box[gi]);
+                root_box(sah_nodes[bi][0], G.blas_box[gi]);
                 const uint32_t nb = (uint32_t)pool.size(), tb = geom[gi].y;
-                for (Node4 nd : sah_nodes[gi]) {
+                for (Node4 nd : sah_nodes[bi]) {
                     int* c = &nd.child.x;
                     const int* k = &nd.cnt.x;
                     for (int q = 0; q < 4; ++q) {
@@ -313,7 +352,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
                     }
                     pool.push_back(nd);
                 }
-                std::copy(sah_order[gi].begin(), sah_order[gi].end(), order_all.begin() + tb);
+                std::copy(sah_order[bi].begin(), sah_order[bi].end(), order_all.begin() + tb);
             }
             if (!pool.empty()) G.blas_nodes.upload(pool.data(), pool.size(), st);
             order.upload(order_all.data(), order_all.size(), st);

@@ -92,13 +92,20 @@ def renderer():
         yield r
 
 
-def test_forward_matches_torch(renderer):
+# (48, 80): every level narrower than one 128-pixel tile (the per-tile conv kernel);
+# (32, 256): levels 0 and 1 at least 128 wide (the persistent halo conv kernel, its
+# backward-data convolutions included), the deeper levels narrow.
+SIZES = [(48, 80), (32, 256)]
+
+
+@pytest.mark.parametrize("h,w", SIZES)
+def test_forward_matches_torch(renderer, h, w):
     import torch
 
     d = api.Denoiser(renderer, seed=3)
     params = d.getParams()
-    wb = [(w.cuda().to(torch.bfloat16).float(), b.cuda()) for w, b in _unpack(params, torch)]
-    n, h, w = 2, 48, 80
+    wb = [(w_.cuda().to(torch.bfloat16).float(), b.cuda()) for w_, b in _unpack(params, torch)]
+    n = 2
     feat, _ = _inputs(torch, n, h, w, 11)
     out = torch.full((n, h, w, 4), 7.0, device="cuda", dtype=torch.float32)
     torch.cuda.synchronize()
@@ -122,7 +129,8 @@ def test_forward_matches_torch(renderer):
     d.close()
 
 
-def test_gradients_match_autograd(renderer):
+@pytest.mark.parametrize("h,w", [(32, 48), (32, 256)])
+def test_gradients_match_autograd(renderer, h, w):
     import torch
 
     d = api.Denoiser(renderer, seed=5)
@@ -135,7 +143,7 @@ def test_gradients_match_autograd(renderer):
         params[o:o + cout] = rng.normal(0.0, 0.05, cout)
         o += cout
     d.setParams(params)
-    n, h, w = 2, 32, 48
+    n = 2
     feat, target = _inputs(torch, n, h, w, 21)
     base = torch.zeros((n, h, w, 4), device="cuda")
     base[..., :3] = torch.asinh(target[..., :3] / 0.1) + 0.3 * torch.randn((n, h, w, 3), device="cuda")
