@@ -353,10 +353,17 @@ KF_API int kf_denoiser_set_params(kf_denoiser d, const float* in, uint64_t count
 KF_API int kf_denoiser_save(kf_denoiser d, const char* path);
 KF_API int kf_denoiser_load(kf_denoiser d, const char* path);
 /* Renders one training pair with camera c of scene s: one frame of low_spp samples
- * (the input) and the running mean of high_frames frames of high_spp (the target).
- * Width and height divisible by 16; all views of a denoiser share one size. */
+ * (the input) and the mean of high_frames frames of high_spp from the FP64
+ * accumulation (the target). Width and height divisible by 16; all views of a
+ * denoiser share one size. No kuafu counterpart (OptiX ships a trained network). */
 KF_API int kf_denoiser_add_view(kf_denoiser d, kf_scene s, kf_camera c, uint32_t low_spp, uint32_t high_spp,
                                 uint32_t high_frames);
+/* As kf_denoiser_add_view with num_inputs inputs (one frame of low_spp[i] samples each,
+ * independent random streams) paired with one shared target: num_inputs training pairs
+ * for the cost of one target render. 1 <= num_inputs <= 64. No kuafu counterpart. */
+KF_API int kf_denoiser_add_view_inputs(kf_denoiser d, kf_scene s, kf_camera c, const uint32_t* low_spp,
+                                       uint32_t num_inputs, uint32_t high_spp, uint32_t high_frames);
+/* Number of training pairs (inputs) added so far. */
 KF_API int kf_denoiser_num_views(kf_denoiser d, uint32_t* out);
 /* iters Adam steps over batch random crops (crop x crop, crop % 16 == 0); *mean_loss may be NULL. */
 KF_API int kf_denoiser_train(kf_denoiser d, uint32_t iters, uint32_t batch, uint32_t crop, float lr,

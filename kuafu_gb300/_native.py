@@ -242,6 +242,7 @@ PROTOTYPES = {
     "kf_denoiser_save": (I, [VP, C.c_char_p]),
     "kf_denoiser_load": (I, [VP, C.c_char_p]),
     "kf_denoiser_add_view": (I, [VP, VP, VP, U32, U32, U32]),
+    "kf_denoiser_add_view_inputs": (I, [VP, VP, VP, C.POINTER(U32), U32, U32, U32]),
     "kf_denoiser_num_views": (I, [VP, C.POINTER(U32)]),
     "kf_denoiser_train": (I, [VP, U32, U32, U32, F, C.POINTER(F)]),
     "kf_denoiser_apply": (I, [VP, VP]),

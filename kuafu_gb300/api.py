@@ -607,6 +607,12 @@ class Denoiser:
         N.check(_lib().kf_denoiser_add_view(self._h, scene._h, cam._h, int(low_spp), int(high_spp),
                                             int(high_frames)))
 
+    def addViewInputs(self, scene: Scene, cam: Camera, low_spps, high_spp: int, high_frames: int = 1):
+        """Several inputs (one frame of each low spp) paired with one shared target."""
+        arr = (C.c_uint32 * len(low_spps))(*[int(k) for k in low_spps])
+        N.check(_lib().kf_denoiser_add_view_inputs(self._h, scene._h, cam._h, arr, len(low_spps), int(high_spp),
+                                                   int(high_frames)))
+
     def numViews(self) -> int:
         n = C.c_uint32()
         N.check(_lib().kf_denoiser_num_views(self._h, C.byref(n)))

@@ -1368,20 +1368,26 @@ KF_API int kf_denoiser_load(kf_denoiser d, const char* path) {
         denoiser_set_params(d, p.data(), n);
     });
 }
-KF_API int kf_denoiser_add_view(kf_denoiser d, kf_scene s, kf_camera c, uint32_t low_spp, uint32_t high_spp,
-                                uint32_t high_frames) {
+KF_API int kf_denoiser_add_view_inputs(kf_denoiser d, kf_scene s, kf_camera c, const uint32_t* low_spp,
+                                       uint32_t num_inputs, uint32_t high_spp, uint32_t high_frames) {
     return guarded([&] {
         check_denoiser(d);
         kf_scene_s* sc = check_scene(s);
         kf_camera_s* cam = check_camera(c);
         REQ(cam->scene == sc, "the camera does not belong to the scene");
-        REQ(low_spp > 0 && high_spp > 0 && high_frames > 0, "sample counts must be positive");
+        REQ(low_spp && num_inputs >= 1 && num_inputs <= 64, "between 1 and 64 inputs per view");
+        for (uint32_t i = 0; i < num_inputs; ++i) REQ(low_spp[i] > 0, "sample counts must be positive");
+        REQ(high_spp > 0 && high_frames > 0, "sample counts must be positive");
         kf_renderer_s* r = denoiser_renderer(d);
         KF_CUDA_CHECK(cudaSetDevice(r->device));
         camera_update_view(cam);
-        denoiser_add_view(d, sc, cam, low_spp, high_spp, high_frames);
+        denoiser_add_view(d, sc, cam, low_spp, num_inputs, high_spp, high_frames);
         r->last_camera = nullptr; // the next run() restarts accumulation
     });
+}
+KF_API int kf_denoiser_add_view(kf_denoiser d, kf_scene s, kf_camera c, uint32_t low_spp, uint32_t high_spp,
+                                uint32_t high_frames) {
+    return kf_denoiser_add_view_inputs(d, s, c, &low_spp, 1, high_spp, high_frames);
 }
 KF_API int kf_denoiser_num_views(kf_denoiser d, uint32_t* out) {
     return guarded([&] {

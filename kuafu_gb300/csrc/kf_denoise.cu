@@ -383,13 +383,14 @@ __global__ void k_gather_crops(const bf16* __restrict__ feat, const float4* __re
         const int x = (int)(i % c);
         const int y = (int)((i / c) % c);
         const int b = (int)(i / ((size_t)c * c));
-        const int4 cr = crops[b]; // {image, y0, x0, -}
+        const int4 cr = crops[b]; // {input, y0, x0, target}
         const size_t src = ((size_t)cr.x * H + cr.y + y) * W + cr.z + x;
+        const size_t src_t = ((size_t)cr.w * H + cr.y + y) * W + cr.z + x;
         const uint4* s = reinterpret_cast<const uint4*>(feat + src * 32);
         uint4* d = reinterpret_cast<uint4*>(bf + i * 32);
         for (int k = 0; k < 4; ++k) d[k] = s[k];
         bb[i] = base[src];
-        bt[i] = tgt[src];
+        bt[i] = tgt[src_t];
     }
 }
 
@@ -445,8 +446,11 @@ struct kf_denoiser_s {
     int step = 0;
     bool packed = false;
     kf::Acts acts;
-    // dataset
-    int ds_h = 0, ds_w = 0, ds_n = 0;
+    // dataset: ds_n inputs (features + residual base), ds_targets targets; input k is
+    // paired with target ds_tgt_of[k]. Capacities grow by doubling.
+    int ds_h = 0, ds_w = 0, ds_n = 0, ds_targets = 0;
+    size_t ds_cap_in = 0, ds_cap_tgt = 0;
+    std::vector<int> ds_tgt_of;
     kf::DeviceBuffer<__nv_bfloat16> ds_feat;
     kf::DeviceBuffer<float4> ds_base, ds_tgt;
     kf::DeviceBuffer<__nv_bfloat16> batch_feat;
@@ -825,8 +829,8 @@ template <class T> void grow(DeviceBuffer<T>& b, size_t old_n, size_t new_n, cud
 }
 } // namespace
 
-void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint32_t low_spp, uint32_t high_spp,
-                       uint32_t high_frames) {
+void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, const uint32_t* low_spp,
+                       uint32_t num_inputs, uint32_t high_spp, uint32_t high_frames) {
     kf_renderer_s* r = d->r;
     cudaStream_t st = r->stream;
     KF_REQUIRE(c->width % 16 == 0 && c->height % 16 == 0, KF_ERR_INVALID_ARGUMENT,
@@ -838,23 +842,37 @@ void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint3
     KF_REQUIRE(c->width == d->ds_w && c->height == d->ds_h, KF_ERR_INVALID_ARGUMENT,
                "all training views must have the same size");
     const size_t npix = (size_t)c->width * c->height;
-    const size_t k = (size_t)d->ds_n;
-    grow(d->ds_feat, npix * 32 * k, npix * 32 * (k + 1), st);
-    grow(d->ds_base, npix * k, npix * (k + 1), st);
-    grow(d->ds_tgt, npix * k, npix * (k + 1), st);
+    const size_t k = (size_t)d->ds_n, t = (size_t)d->ds_targets;
+    if (k + num_inputs > d->ds_cap_in) {
+        const size_t cap = std::max<size_t>({k + num_inputs, 2 * d->ds_cap_in, 8});
+        grow(d->ds_feat, npix * 32 * k, npix * 32 * cap, st);
+        grow(d->ds_base, npix * k, npix * cap, st);
+        d->ds_cap_in = cap;
+    }
+    if (t + 1 > d->ds_cap_tgt) {
+        const size_t cap = std::max<size_t>({t + 1, 2 * d->ds_cap_tgt, 8});
+        grow(d->ds_tgt, npix * t, npix * cap, st);
+        d->ds_cap_tgt = cap;
+    }
     FrameStateGuard guard(r);
     r->cfg.accumulate_frames = 1;
-    // noisy input: one frame of low_spp samples
-    r->frame_count = -1;
-    render_frame(r, s, c, low_spp);
-    camera_features(c, low_spp, d->ds_feat.ptr + npix * 32 * k, d->ds_base.ptr + npix * k, c->height, c->width, st);
+    // noisy inputs: one frame of low_spp[i] samples each (every render takes a new frame
+    // index, so the inputs' random streams and the target's are independent)
+    for (uint32_t i = 0; i < num_inputs; ++i) {
+        r->frame_count = -1;
+        render_frame(r, s, c, low_spp[i]);
+        camera_features(c, low_spp[i], d->ds_feat.ptr + npix * 32 * (k + i), d->ds_base.ptr + npix * (k + i),
+                        c->height, c->width, st);
+    }
     // target: high_frames frames of high_spp samples, averaged from the FP64 accumulation
     r->frame_count = -1;
     for (uint32_t f = 0; f < high_frames; ++f) render_frame(r, s, c, high_spp);
-    k_target_from_sum64<<<grid_for(npix), 256, 0, st>>>(c->sum64.ptr, npix, d->ds_tgt.ptr + npix * k);
+    k_target_from_sum64<<<grid_for(npix), 256, 0, st>>>(c->sum64.ptr, npix, d->ds_tgt.ptr + npix * t);
     KF_CUDA_CHECK(cudaGetLastError());
     KF_CUDA_CHECK(cudaStreamSynchronize(st));
-    ++d->ds_n;
+    for (uint32_t i = 0; i < num_inputs; ++i) d->ds_tgt_of.push_back((int)t);
+    d->ds_n += (int)num_inputs;
+    ++d->ds_targets;
 }
 
 float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32_t crop, float lr) {
@@ -874,7 +892,7 @@ float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32
             cr[b].x = (int)(d->rng() % (uint32_t)d->ds_n);
             cr[b].y = (int)(d->rng() % (uint32_t)(d->ds_h - crop + 1));
             cr[b].z = (int)(d->rng() % (uint32_t)(d->ds_w - crop + 1));
-            cr[b].w = 0;
+            cr[b].w = d->ds_tgt_of[(size_t)cr[b].x];
         }
         d->crops.upload(cr.data(), batch, st);
         k_gather_crops<<<grid_for(per * batch), 256, 0, st>>>(d->ds_feat.ptr, d->ds_base.ptr, d->ds_tgt.ptr, d->ds_h,

@@ -28,9 +28,10 @@ void denoiser_forward(kf_denoiser_impl* d, const void* feat, const void* base, i
 float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const void* base, const float* tgt, int n, int h,
                           int w, float lr, float* grads_out, bool apply_update);
 
-// Renders one training pair of a camera: a low_spp frame (input) and high_frames x high_spp (target).
-void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, uint32_t low_spp, uint32_t high_spp,
-                       uint32_t high_frames);
+// Renders training pairs of a camera: one frame of low_spp[i] samples per input and one
+// target (high_frames x high_spp, FP64 accumulation) that all num_inputs inputs share.
+void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, const uint32_t* low_spp,
+                       uint32_t num_inputs, uint32_t high_spp, uint32_t high_frames);
 // Adam over random crops of the training views; returns the mean loss of the iterations.
 float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32_t crop, float lr);
 // Denoises the camera's accumulated radiance into its denoised target.

@@ -13,10 +13,12 @@ at 1920x1080, path depth 5, no Russian roulette. The experiment, all on one GPU:
    `plain_checkpoint_step` samples after that, until the raw relMSE reaches the
    smallest threshold (or `plain_max_spp`); cumulative GPU time of the frames
    from CUDA events (the checkpoints' relMSE evaluations are not counted).
-3. Learned denoiser: trained on this renderer's own pairs (Cornell variations at
-   256x256, inputs cycling 1..1024 spp, targets at 4096 spp), then applied to
-   single frames of k spp of the held-out scene; time = render + denoise (CUDA
-   events).
+3. Learned denoiser: trained in the run on this renderer's own pairs (Cornell
+   variations seen through 256x256 windows of the 1920x1080 view, inputs cycling
+   1..1024 spp, targets at 4096 spp), then applied to single frames of k spp of the
+   held-out scene; time = render + denoise (CUDA events). With `shipped` set, the
+   network shipped with the package (train_network: 2000 windows, 4-spp inputs plus
+   one more input per window, 4096-spp targets) is evaluated on the same frames.
 4. For each threshold tau: the measured time plain accumulation needs to reach raw
    relMSE <= tau and the time the denoised form needs (smallest k whose denoised
    frame reaches tau), and their ratio. "Debiased" values (raw minus ref_floor)
@@ -26,6 +28,7 @@ relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2), reduced
 in FP64 on the GPU (kf_relmse).
 
   python -m kuafu_gb300.denoise_eval [--small] [--json out.json]
+  python -m kuafu_gb300.denoise_eval --train-network kuafu_gb300/weights/unet_cornell_2000x256.kfw
 """
 from __future__ import annotations
 
@@ -109,11 +112,102 @@ def _accumulate(r, cfg, cam, seed, spp_total, frame_spp):
     return _fp64_mean(r, cam)
 
 
+def window_camera(cam: api.Camera, size: int, full_w: int, full_h: int, x0: int, y0: int, fov_deg=40.0):
+    """Makes cam a size x size camera that sees pixels [x0, x0 + size) x [y0, y0 + size) of
+    the full_w x full_h pinhole view of the same pose: same focal length, principal point
+    moved by the window's origin (kuafu's projection, src/core/camera.cpp:111-124, puts
+    pixel u at fx * X / -Z + cx). Training crops are then rendered at the scale of the
+    1080p frames the network denoises, for the cost of the crop."""
+    fy = (full_h / 2.0) / math.tan(math.radians(fov_deg) / 2.0)
+    cam.setFullPerspective(size, size, fy, fy, full_w / 2.0 - x0, full_h / 2.0 - y0, 0.0)
+
+
+def add_training_views(r: api.Kuafu, cfg: api.Config, d: api.Denoiser, count: int, size: int, full_w: int,
+                       full_h: int, inputs_of, high_spp: int, high_frames: int, first: int = 0, log=None) -> float:
+    """Adds `count` training views: seeded Cornell variations (scenes.cornell variation
+    1000 + v), each seen through a size x size window at a seeded place of the full_w x
+    full_h view, with inputs of inputs_of(v) spp and one target of high_frames x high_spp
+    samples (FP64 accumulation). Each view's scene is removed once its pairs are stored.
+    Returns the seconds taken."""
+    rng = scenes.SplitMix64(0x5EED0000 + first)
+    t0 = time.perf_counter()
+    for v in range(first, first + count):
+        s = r.createScene()
+        c = scenes.cornell(r, size, size, scene=s, variation=1000 + v)
+        x0 = min(full_w - size, int(rng.uniform() * (full_w - size + 1)))
+        y0 = min(full_h - size, int(rng.uniform() * (full_h - size + 1)))
+        window_camera(c, size, full_w, full_h, x0, y0)
+        cfg.setSeed(50000 + v)
+        r.applyConfig()
+        d.addViewInputs(s, c, inputs_of(v), high_spp, high_frames)
+        r.removeScene(s)
+        if log and (v - first + 1) % 200 == 0:
+            log(f"training views: {v - first + 1} of {count} ({time.perf_counter() - t0:.0f} s)")
+    return time.perf_counter() - t0
+
+
+def _train(r: api.Kuafu, d: api.Denoiser, iters: int, batch: int, crop: int, lr: float) -> list:
+    """Adam over random crops; lr x 0.1 for the last 20 % of the steps. Mean loss per tenth."""
+    losses, done, chunk = [], 0, max(1, iters // 10)
+    while done < iters:
+        k = min(chunk, iters - done)
+        losses.append(d.train(k, batch, crop, lr * (0.1 if done >= 0.8 * iters else 1.0)))
+        done += k
+    r.synchronize()
+    return losses
+
+
+def _denoised_frames(r, cfg, cam, d, spps, ref, floor, timer, flops, log, seed=9):
+    """Single frames of k spp of the current scene, denoised by d: times and relMSE."""
+    den = []
+    for k in spps:
+        cfg.setSeed(seed)
+        cfg.setPerPixelSampleRate(k)
+        cfg.setAccumulatingFrames(False)
+        r.applyConfig()
+        r.resetFrame()
+        r.run()  # capture
+        d.apply(cam)
+        r.synchronize()
+        with timer:
+            r.run()
+        t_render = timer.ms
+        noisy = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
+        with timer:
+            d.apply(cam)
+        t_dn = timer.ms
+        out = r.downloadAov(cam, N.KF_AOV_DENOISED_F32)
+        e_n = _gpu_relmse(r, noisy, ref)
+        e_d = _gpu_relmse(r, out, ref)
+        den.append({"spp": k, "render_ms": t_render, "denoise_ms": t_dn, "ms": t_render + t_dn,
+                    "relmse_noisy": e_n, "relmse": e_d, "relmse_debiased": e_d - floor,
+                    "denoise_tflops": flops / (t_dn / 1e3) / 1e12})
+        log(f"denoised {k} spp: noisy {e_n:.3e} -> {e_d:.3e} ({t_render:.1f} + {t_dn:.1f} ms)")
+    return den
+
+
+def _time_to(plain, den, thresholds):
+    """For each threshold: measured plain time, denoised time, ratio (raw and debiased relMSE)."""
+    ttr = []
+    for tau in thresholds:
+        row = {"tau": tau}
+        for key in ("relmse", "relmse_debiased"):
+            hit = next((p for p in plain if p[key] <= tau), None)
+            pt, how = (hit["ms"], "measured") if hit is not None else (None, "not reached")
+            dh = [p for p in den if p[key] <= tau]
+            dt = min(p["ms"] for p in dh) if dh else None
+            dk = min((p for p in dh), key=lambda p: p["ms"])["spp"] if dh else None
+            row[key] = {"plain_ms": pt, "plain": how, "plain_spp": hit["spp"] if hit else None, "denoised_ms": dt,
+                        "denoised_input_spp": dk, "speedup": (pt / dt) if (pt and dt) else None}
+        ttr.append(row)
+    return ttr
+
+
 def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_spp=8, plain_checkpoint_step=2048,
         plain_max_spp=65536, train_views=66, train_size=256, train_high_spp=64,
         train_high_frames=64, train_iters=4000, train_batch=8, train_crop=128, lr=1e-3,
         denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3),
-        depth=5, log=print) -> dict:
+        depth=5, shipped=None, save_trained=None, log=print) -> dict:
     cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
     res = {"scene": "cornell", "width": width, "height": height, "depth": depth, "eps": EPS}
     with api.Kuafu(cfg) as r:
@@ -162,85 +256,108 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
         ms_per_spp = plain[-1]["ms"] / plain[-1]["spp"]
         res["plain_fit"] = {"ms_per_spp": ms_per_spp}
 
-        # 3. denoiser training on Cornell variations
+        # 3. denoiser training on Cornell variations seen through train_size windows of
+        #    the width x height view
         d = api.Denoiser(r, seed=0)
+        t_data = add_training_views(r, cfg, d, train_views, train_size, width, height,
+                                    lambda v: [denoise_spps[v % len(denoise_spps)]], train_high_spp,
+                                    train_high_frames)
         t0 = time.perf_counter()
-        for v in range(train_views):
-            s = r.createScene()
-            c = scenes.cornell(r, train_size, train_size, scene=s, variation=1000 + v)
-            cfg.setSeed(50000 + v)
-            r.applyConfig()
-            d.addView(s, c, denoise_spps[v % len(denoise_spps)], train_high_spp, train_high_frames)
-        t_data = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        losses = []
-        chunk = max(1, train_iters // 10)
-        done = 0
-        while done < train_iters:
-            k = min(chunk, train_iters - done)
-            cur_lr = lr * (0.1 if done >= 0.8 * train_iters else 1.0)
-            losses.append(d.train(k, train_batch, train_crop, cur_lr))
-            done += k
-        r.synchronize()
+        losses = _train(r, d, train_iters, train_batch, train_crop, lr)
         t_train = time.perf_counter() - t0
-        res["training"] = {"views": train_views, "size": train_size, "input_spp": list(denoise_spps),
-                           "target_spp": train_high_spp * train_high_frames, "iters": train_iters,
-                           "batch": train_batch, "crop": train_crop, "lr": lr, "loss_curve": losses,
-                           "data_seconds": t_data, "train_seconds": t_train}
+        res["training"] = {"views": train_views, "size": train_size, "windows_of": [width, height],
+                           "input_spp": list(denoise_spps), "target_spp": train_high_spp * train_high_frames,
+                           "iters": train_iters, "batch": train_batch, "crop": train_crop, "lr": lr,
+                           "loss_curve": losses, "data_seconds": t_data, "train_seconds": t_train}
         log(f"training: data {t_data:.1f} s, {train_iters} iters {t_train:.1f} s, loss {losses[0]:.4f} -> "
             f"{losses[-1]:.4f}")
+        if save_trained:
+            d.save(save_trained)
 
         # 4. denoised single frames of the held-out scene
         r.setScene(scene)
-        den = []
         flops = unet_flops(height, width)
-        for k in denoise_spps:
-            cfg.setSeed(9)
-            cfg.setPerPixelSampleRate(k)
-            cfg.setAccumulatingFrames(False)
-            r.applyConfig()
-            r.resetFrame()
-            r.run()  # capture
-            d.apply(cam)
-            r.synchronize()
-            with timer:
-                r.run()
-            t_render = timer.ms
-            noisy = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32)
-            with timer:
-                d.apply(cam)
-            t_dn = timer.ms
-            out = r.downloadAov(cam, N.KF_AOV_DENOISED_F32)
-            e_n = _gpu_relmse(r, noisy, ref)
-            e_d = _gpu_relmse(r, out, ref)
-            den.append({"spp": k, "render_ms": t_render, "denoise_ms": t_dn, "ms": t_render + t_dn,
-                        "relmse_noisy": e_n, "relmse": e_d, "relmse_debiased": e_d - floor,
-                        "denoise_tflops": flops / (t_dn / 1e3) / 1e12})
-            log(f"denoised {k} spp: noisy {e_n:.3e} -> {e_d:.3e} ({t_render:.1f} + {t_dn:.1f} ms)")
+        den = _denoised_frames(r, cfg, cam, d, denoise_spps, ref, floor, timer, flops, log)
         res["denoised"] = den
         res["denoiser_flops_per_frame"] = flops
         d.close()
+        # the network shipped with the package (trained by train_network), same frames
+        if shipped:
+            d2 = api.Denoiser(r, seed=0)
+            d2.load(shipped)
+            log("shipped network:")
+            den2 = _denoised_frames(r, cfg, cam, d2, denoise_spps, ref, floor, timer, flops, log)
+            res["shipped"] = {"weights": str(shipped), "denoised": den2,
+                              "time_to_relmse": _time_to(plain, den2, thresholds)}
+            d2.close()
 
     # 5. time to each threshold: measured on both arms, raw relMSE (debiased beside it)
-    ttr = []
-    for tau in thresholds:
-        row = {"tau": tau}
-        for key in ("relmse", "relmse_debiased"):
-            hit = next((p for p in plain if p[key] <= tau), None)
-            pt, how = (hit["ms"], "measured") if hit is not None else (None, "not reached")
-            dh = [p for p in den if p[key] <= tau]
-            dt = min(p["ms"] for p in dh) if dh else None
-            dk = min((p for p in dh), key=lambda p: p["ms"])["spp"] if dh else None
-            row[key] = {"plain_ms": pt, "plain": how, "plain_spp": hit["spp"] if hit else None, "denoised_ms": dt,
-                        "denoised_input_spp": dk, "speedup": (pt / dt) if (pt and dt) else None}
-        ttr.append(row)
-    res["time_to_relmse"] = ttr
+    res["time_to_relmse"] = _time_to(plain, den, thresholds)
     floor_4096 = floor * ref_spp / 4096.0  # the floor falls as 1 / spp
     res["note_4096spp_reference"] = (
         f"against a 4096-spp reference the floor would be about {floor_4096:.2e} (the relMSE of an independent "
         f"estimate includes the reference's own noise), so nothing could be measured below 1e-3 against it; the "
         f"reference here has {ref_spp} spp")
     return res
+
+
+def train_network(path, views=2000, size=256, full_w=1920, full_h=1080, base_spp=4,
+                  extra_spps=(1, 2, 8, 16, 32, 64, 128, 256, 512, 1024), high_spp=256, high_frames=16, iters=10000,
+                  batch=16, crop=128, lr=1e-3, depth=5, seed=0, log=print) -> dict:
+    """Trains the network shipped with the package and saves it to `path`.
+
+    Training set: `views` Cornell variations, each a size x size window of the
+    full_w x full_h view (window_camera), with two inputs — one frame of `base_spp`
+    samples and one of extra_spps[v % len] — sharing one target of high_frames x
+    high_spp samples from the FP64 accumulation (defaults: 2000 crops of 256x256,
+    4-spp inputs, 4096-spp targets; the second input covers the 1..1024-spp frames the
+    time-to-relMSE experiment denoises). Adam over random crop x crop crops."""
+    cfg = scenes.cornell_config(spp=high_spp, depth=depth)
+    with api.Kuafu(cfg) as r:
+        d = api.Denoiser(r, seed=seed)
+        t_data = add_training_views(r, cfg, d, views, size, full_w, full_h,
+                                    lambda v: [base_spp, extra_spps[v % len(extra_spps)]], high_spp, high_frames,
+                                    log=log)
+        log(f"{d.numViews()} training pairs from {views} views in {t_data:.0f} s")
+        t0 = time.perf_counter()
+        losses = _train(r, d, iters, batch, crop, lr)
+        t_train = time.perf_counter() - t0
+        log(f"{iters} Adam steps in {t_train:.0f} s, loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+        d.save(path)
+        d.close()
+    return {"views": views, "pairs": 2 * views, "size": size, "windows_of": [full_w, full_h],
+            "input_spp": [base_spp] + list(extra_spps), "target_spp": high_spp * high_frames, "iters": iters,
+            "batch": batch, "crop": crop, "lr": lr, "loss_curve": losses, "data_seconds": t_data,
+            "train_seconds": t_train}
+
+
+def icosphere_eval(networks: dict, width=1920, height=1080, ref_spp=2048, ref_frame_spp=32,
+                   spps=(1, 4, 8, 32, 128), log=print) -> dict:
+    """The networks (name -> parameter file) on content they were not trained on: the
+    256-icosphere scene (glossy, metallic and transmissive spheres, 7 lights, RR, depth 8)
+    at width x height. Reference: two FP64 accumulations of ref_spp / 2 (floor as in run())."""
+    cfg = scenes.icosphere_config(spp=ref_frame_spp, depth=8)
+    cfg.setRussianRoulette(True)
+    out = {"scene": f"256 icospheres {width}x{height} depth 8", "reference_spp": ref_spp}
+    with api.Kuafu(cfg) as r:
+        cam = scenes.icospheres(r, width, height)
+        a = _accumulate(r, cfg, cam, 2001, ref_spp // 2, ref_frame_spp)
+        b = _accumulate(r, cfg, cam, 2002, ref_spp // 2, ref_frame_spp)
+        ref = 0.5 * (a + b)
+        floor = _gpu_relmse(r, a, b) / 4.0
+        out["ref_floor"] = floor
+        log(f"icosphere reference {ref_spp} spp: floor {floor:.3e}")
+        del a, b
+        timer = _Timer(r)
+        flops = unet_flops(height, width)
+        for name, path in networks.items():
+            d = api.Denoiser(r, seed=0)
+            d.load(path)
+            log(f"{name} network on the icosphere scene:")
+            den = _denoised_frames(r, cfg, cam, d, spps, ref, floor, timer, flops, log)
+            out[name] = [{k: p[k] for k in ("spp", "relmse_noisy", "relmse", "relmse_debiased")} for p in den]
+            d.close()
+    return out
 
 
 SMALL = dict(width=480, height=272, ref_spp=4096, plain_max_spp=8192, plain_checkpoint_step=512, train_views=18, train_iters=300,
@@ -253,7 +370,22 @@ def main(argv=None):
     ap.add_argument("--json", default=None)
     ap.add_argument("--train-iters", type=int, default=None)
     ap.add_argument("--ref-spp", type=int, default=None)
+    ap.add_argument("--train-network", metavar="PATH", default=None,
+                    help="train the shipped network (2000 windows of 256x256, 4-spp inputs, 4096-spp targets) "
+                         "and save it to PATH instead of running the experiment")
+    ap.add_argument("--views", type=int, default=2000, help="training views of --train-network")
     a = ap.parse_args(argv)
+    if a.train_network:
+        kw = {"views": a.views}
+        if a.train_iters:
+            kw["iters"] = a.train_iters
+        res = train_network(a.train_network, **kw)
+        s = json.dumps(res)
+        if a.json:
+            with open(a.json, "w") as f:
+                f.write(s)
+        print(s)
+        return
     kw = dict(SMALL) if a.small else {}
     if a.train_iters:
         kw["train_iters"] = a.train_iters

@@ -264,3 +264,30 @@ def test_denoiser_beats_noisy_input_on_cornell():
         r.setDenoiser(None)
         d.close()
         assert np.isfinite(den2).all()
+
+
+def test_views_with_shared_targets():
+    """kf_denoiser_add_view_inputs: several inputs per view share one target; the scene
+    can go once its pairs are stored; bad input lists are refused."""
+    cfg = scenes.cornell_config(spp=4, depth=5)
+    with api.Kuafu(cfg) as r:
+        d = api.Denoiser(r, seed=0)
+        for v in range(3):
+            s = r.createScene()
+            cam = scenes.cornell(r, 32, 32, scene=s, variation=200 + v)
+            d.addViewInputs(s, cam, [1, 4, 16], 16, 2)
+            r.removeScene(s)
+        assert d.numViews() == 9
+        s = r.createScene()
+        cam = scenes.cornell(r, 32, 32, scene=s, variation=300)
+        with pytest.raises(N.KfError):
+            d.addViewInputs(s, cam, [], 16, 1)
+        with pytest.raises(N.KfError):
+            d.addViewInputs(s, cam, [4, 0], 16, 1)
+        with pytest.raises(N.KfError):
+            d.addViewInputs(s, cam, [1] * 65, 16, 1)
+        assert d.numViews() == 9
+        loss = d.train(5, batch=4, crop=32, lr=1e-3)
+        assert np.isfinite(loss)
+        assert _tc_error() == 0
+        d.close()
