@@ -87,6 +87,7 @@ struct SceneGpu {
     uint64_t built_env_version = 0;
     std::vector<uint32_t> blas_root;                 // per geometry
     std::vector<std::array<float, 6>> blas_box;      // per geometry object-space box
+    std::vector<std::vector<float>> blas_hull;      // per geometry: xyz points bounding its triangles
     std::vector<uint32_t> tri_offset, vert_offset;   // per geometry
     uint64_t built_geom_stamp = 0;
     uint64_t built_inst_stamp = 0;
