@@ -121,12 +121,50 @@ def build_scene(device: int, profile=False, debug=False):
         cfg.setBvhBuilder(WORKLOAD["bvh_builder"])
     if "blas_leaf_size" in WORKLOAD:
         cfg.setBlasLeafSize(WORKLOAD["blas_leaf_size"])
+    if "blas_share" in WORKLOAD:
+        cfg.setBlasShare(WORKLOAD["blas_share"])
     if "dyn_refill_below" in WORKLOAD or "dyn_steps" in WORKLOAD:
         cfg.setDynamicFetch(WORKLOAD.get("dyn_refill_below", 16), WORKLOAD.get("dyn_steps", 32))
     r = api.Kuafu(cfg)
     cam = scenes.icospheres(r, WORKLOAD["width"], WORKLOAD["height"], count=WORKLOAD["count"],
                             level=WORKLOAD["level"], seed=WORKLOAD["seed"])
     return r, cam
+
+
+def separate_blas_summary(device: int, steps: int = 5) -> dict:
+    """The same frame with blas_share = 0: every icosphere geometry keeps its own copy of
+    the BLAS nodes and triangles (256 copies, ~150 MB against the 129 MB L2) instead of the
+    default one shared copy. Same hits and radiance; CUDA-event frame times after an L2
+    flush, as for the headline."""
+    import torch
+
+    WORKLOAD["blas_share"] = 0
+    try:
+        r, _ = build_scene(device)
+    finally:
+        del WORKLOAD["blas_share"]
+    stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", device))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    for _ in range(2):
+        r.run()
+    r.synchronize()
+    nodes = r.stats().blas_nodes
+    r.resetStats()
+    ms = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        r.run()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    st = r.stats()
+    rays = st.rays_primary + st.rays_extension + st.rays_shadow
+    r.close()
+    return {"mrays_s": rays / (sum(ms) / 1e3) / 1e6, "ms_per_step": statistics.median(ms), "blas_nodes": nodes}
 
 
 def cpu_baseline_sample(seconds_target=12.0, threads=0):
@@ -516,6 +554,8 @@ def run_ours(args):
                 traffic = json.loads(tf.read_text()).get(kname + " dram_bytes_per_launch")
             except Exception:
                 traffic = None
+        shared_nodes = sp.blas_nodes
+        separate = separate_blas_summary(device)
         cpu = cpu_baseline_sample()
         # single-GPU experiments: run once, at N = 1 (under torchrun the other ranks would idle)
         ttr = None if (args.no_denoise or ws > 1) else time_to_relmse_summary()
@@ -542,6 +582,10 @@ def run_ours(args):
                                                       max(sc.rays_shadow, 1))),
                          "kernel_ms_per_frame": {"extend": sp.extend_ms, "shade": sp.shade_ms,
                                                  "shadow": sp.shadow_ms, "frame": sp.frame_ms}},
+            "blas": {"shared": {"blas_nodes": shared_nodes,
+                                "note": "the 256 geometries have identical positions and indices (one material "
+                                        "each) and share one BLAS copy (blas_share = 1, the default)"},
+                     "separate": separate},
             "bvh_build_ms": {"default (host binned SAH, 256 BLAS + TLAS)": build_ms,
                              "gpu_lbvh (256 BLAS + TLAS)": lbvh_ms},
             "cpu_baseline": cpu,
@@ -585,6 +629,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 128-view workload")
     ap.add_argument("--bvh-builder", type=int, default=None, help="0: GPU LBVH, 1: host binned SAH")
     ap.add_argument("--leaf", type=int, default=None, help="BLAS leaf size")
+    ap.add_argument("--blas-share", type=int, default=None, help="1: identical geometries share one BLAS (default)")
     ap.add_argument("--dyn", type=int, nargs=2, default=None, metavar=("REFILL_BELOW", "STEPS"),
                     help="persistent traversal scheduling")
     ap.add_argument("--profile-denoiser", type=int, default=0, metavar="N",
@@ -596,6 +641,8 @@ def main():
         WORKLOAD["bvh_builder"] = args.bvh_builder
     if args.leaf is not None:
         WORKLOAD["blas_leaf_size"] = args.leaf
+    if args.blas_share is not None:
+        WORKLOAD["blas_share"] = args.blas_share
     if args.dyn is not None:
         WORKLOAD["dyn_refill_below"], WORKLOAD["dyn_steps"] = args.dyn
     if args.warmup < 3:

@@ -90,6 +90,10 @@ typedef struct kf_config {
                                       lanes than this are busy (1..32, default 16) */
     uint32_t dyn_steps;            /* ... and runs this many traversal steps between fetches
                                       (1..64, default 32) */
+    uint32_t blas_share;           /* 1 (default): geometries with identical positions and
+                                      indices (materials may differ) share one BLAS in the
+                                      node and triangle pools; 0: one copy per geometry.
+                                      Host SAH builds only. Same hits either way. */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */

@@ -93,7 +93,7 @@ class kf_config(C.Structure):
                 ("tlas_leaf_size", C.c_uint32), ("max_paths_in_flight", C.c_uint64), ("debug_outputs", C.c_uint32),
                 ("profile", C.c_uint32), ("use_graph", C.c_uint32), ("device", C.c_uint32),
                 ("host_only", C.c_uint32), ("traversal", C.c_uint32), ("bvh_builder", C.c_uint32),
-                ("dyn_refill_below", C.c_uint32), ("dyn_steps", C.c_uint32)]
+                ("dyn_refill_below", C.c_uint32), ("dyn_steps", C.c_uint32), ("blas_share", C.c_uint32)]
 
 
 class kf_stats(C.Structure):

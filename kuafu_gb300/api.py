@@ -73,6 +73,8 @@ class Config:
     def setHostOnly(self, flag): self._c.host_only = int(bool(flag))
     def setTraversal(self, mode): self._c.traversal = int(mode)
     def setBvhBuilder(self, mode): self._c.bvh_builder = int(mode)
+
+    def setBlasShare(self, on): self._c.blas_share = int(bool(on))
     def setDynamicFetch(self, refill_below=16, steps=32):
         self._c.dyn_refill_below, self._c.dyn_steps = int(refill_below), int(steps)
 

@@ -212,6 +212,7 @@ KF_API void kf_config_init(kf_config* c) {
     c->bvh_builder = 1;
     c->dyn_refill_below = 16;
     c->dyn_steps = 32;
+    c->blas_share = 1;
 }
 
 KF_API int kf_renderer_create(const kf_config* cfg, kf_renderer* out) {

@@ -90,6 +90,7 @@ struct SceneGpu {
     std::vector<std::vector<float>> blas_hull;      // per geometry: xyz points bounding its triangles
     std::vector<uint32_t> tri_offset, vert_offset;   // per geometry
     uint64_t built_geom_stamp = 0;
+    uint32_t built_bvh_key = 0;  // builder, leaf size and sharing the BLAS were built with
     uint64_t built_inst_stamp = 0;
     uint64_t built_xform_stamp = 0;
     std::vector<kf::Node4> tlas_host_nodes; // TLAS topology kept for refits

@@ -244,7 +244,9 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         KF_CUDA_CHECK(cudaEventRecord(e0, st));
     }
     bool built_any = false, refitted = false;
-    if (G.built_geom_stamp != s->geom_stamp) {
+    const uint32_t bvh_key = 1u | (r->cfg.bvh_builder << 1) | (r->cfg.blas_leaf_size << 2) |
+                             ((r->cfg.blas_share ? 1u : 0u) << 8);
+    if (G.built_geom_stamp != s->geom_stamp || G.built_bvh_key != bvh_key) {
         built_any = true;
         rebuilt_geom = true;
         const size_t ng = s->geometries.size();
@@ -307,8 +309,9 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         std::vector<std::vector<Node4>> sah_nodes(sah ? ng : 0);
         std::vector<std::vector<uint32_t>> sah_order(sah ? ng : 0);
         // geometries whose triangles are byte-identical (same positions and indices, the
-        // materials may differ) share one build; each still gets its own copy of the nodes
-        // and triangles, so the traversal is the same as with separate builds
+        // materials may differ) share one build; with blas_share they also share one copy
+        // of its nodes and triangles (a triangle carries its geometry-local primitive id,
+        // the instance names the geometry, so the hit is the same), else each gets its own
         std::vector<size_t> build_of(ng);
         std::vector<size_t> to_build;
         if (sah) {
@@ -377,9 +380,15 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             std::vector<Node4> pool;
             pool.reserve(total_nodes_est);
             std::vector<uint32_t> order_all(std::max<size_t>(nt, 1), 0u);
+            const bool share = r->cfg.blas_share != 0;
             for (size_t gi = 0; gi < ng; ++gi) {
                 if (geom[gi].z == 0) continue;
                 const size_t bi = build_of[gi];
+                if (share && bi != gi) { // the first geometry of this build was placed before
+                    G.blas_root[gi] = G.blas_root[bi];
+                    G.blas_box[gi] = G.blas_box[bi];
+                    continue;
+                }
                 G.blas_root[gi] = (uint32_t)pool.size();
                 root_box(sah_nodes[bi][0], G.blas_box[gi]);
                 const uint32_t nb = (uint32_t)pool.size(), tb = geom[gi].y;
@@ -434,6 +443,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         }
         G.blas_node_count = node_base;
         G.built_geom_stamp = s->geom_stamp;
+        G.built_bvh_key = bvh_key;
     }
     if (G.built_material_version != g_material_version || rebuilt_geom) {
         std::vector<kf_material_gpu> mats = flatten_materials();

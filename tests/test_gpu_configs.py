@@ -165,6 +165,30 @@ def test_gpu_lbvh_on_the_full_icosphere_scene():
     assert np.array_equal(res[0]["t"][hit], res[1]["t"][hit])
 
 
+def test_shared_blas_gives_the_same_frame():
+    """blas_share: the 256 identical icosphere geometries (one material each) share one BLAS
+    copy instead of 256; the frame's hits and per-path radiance are bit-identical, and the
+    node pool holds one sphere's nodes."""
+    spp, depth, w, h = 2, 6, 320, 180
+    res, nodes = [], []
+    for share in (0, 1):
+        cfg = scenes.icosphere_config(spp=spp, depth=depth, count=256)
+        cfg.setDebugOutputs(True)
+        cfg.setBlasShare(share)
+        with api.Kuafu(cfg) as r:
+            cam = scenes.icospheres(r, w, h, count=256, level=4, seed=0)
+            r.run()
+            res.append((r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp),
+                        r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, spp)))
+            nodes.append(r.stats().blas_nodes)
+    (h0, p0), (h1, p1) = res
+    for f in ("instance", "prim", "t", "u", "v"):
+        assert np.array_equal(h0[f], h1[f]), f
+    assert (h0["instance"] != 0xFFFFFFFF).mean() > 0.2
+    assert np.array_equal(p0, p1)
+    assert nodes[1] * 200 < nodes[0]
+
+
 def test_converged_fp64_accumulation_against_fp64_oracle():
     """The FP64 sum target (KF_AOV_SUM_F64) over 64 frames x 16 spp = 1024 spp of a 48x48
     Cornell view against the oracle's FP64 render of the same frames. Same sample streams:
