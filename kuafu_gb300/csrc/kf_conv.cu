@@ -228,13 +228,16 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 //
 // A tile is R output rows x 128 pixels x n_tile output channels: R accumulators of
 // n_tile TMEM columns, double-buffered so the epilogue of one tile overlaps the MMAs of
-// the next. Per chunk of CK input channels one 5D TMA box brings the tile's input halo,
-// (R + 2) rows x 130 pixels, into shared memory as [row][channel group][pixel][8 channels]: a
-// K-major operand without swizzle (8 pixels x 16 bytes per core matrix, core matrices
-// 128 bytes apart along M and 130 x 16 bytes apart along K). The A operand of tap
-// (dy, dx) for output row r is that buffer viewed from row r + dy + 1, pixel dx + 1 on:
-// a descriptor offset, so the halo is read from L2 once per chunk and used by all 9
-// taps (the per-tap kernel above reads 9 shifted boxes). The weights of a chunk
+// the next. Per chunk of CK input channels one 4D TMA box brings the tile's input halo,
+// (R + 2) rows x 130 pixels, into shared memory as [row][pixel][CK channels]: one swizzled
+// K-major row of CK x 2 bytes (32- or 64-byte swizzle) per pixel, so TMA moves 32- or
+// 64-byte pieces of the NHWC input (16-byte pieces deliver half the bytes per second).
+// The A operand of tap (dy, dx) for output row r is that buffer viewed from row r + dy,
+// pixel dx on: the descriptor's start address moves by whole rows. The tensor cores apply
+// the swizzle to the absolute shared-memory address, as TMA does when it writes a box at
+// a 1024-byte aligned address, so a view starting at any row reads the rows TMA wrote
+// (the descriptor's base-offset field stays 0). The halo is read from L2 once per chunk
+// and used by all 9 taps (the per-tap kernel above reads 9 shifted boxes). The weights of a chunk
 // ([tap][n_tile][CK], swizzled rows of CK channels) stream with the halo by TMA, or,
 // when one chunk covers all input channels, are loaded once per CTA.
 //
@@ -256,6 +259,7 @@ struct HaloParams {
     int n_tile, R, kchunks;
     int tiles_x, tiles_y, num_tiles;
     int w_resident;          // 1: the weights of all input channels are one chunk, loaded once
+    int stack;               // output rows one MMA covers (1..3, stack x n_tile <= 256)
     uint32_t halo_bytes;     // bytes of one halo box
     uint32_t halo_stride;    // its slot in shared memory (1024-aligned)
     uint32_t w_bytes;        // bytes of one chunk of weights (9 x n_tile x CK)
@@ -269,14 +273,57 @@ struct HaloParams {
     __nv_bfloat16* pool_out;   // fused 2x2 average pooling into a dense [N][H/2][W/2][Cout] tensor, or null
 };
 
-template <int CK>
+// Constants of the MMA sequence that depend on n_tile: weight block offsets (in
+// descriptor units of 16 bytes), instruction descriptors for 1..3 stacked rows, and the
+// TMEM column of each output row.
+struct HaloMmaConsts {
+    uint32_t boff[9];
+    uint32_t idesc[3];
+    uint32_t dcol[4];
+};
+
+// The MMAs of one chunk, unrolled at compile time (the single issuing thread then spends a
+// few instructions per MMA; built from a table at run time they took half again as long).
+// Halo row hr with shift dx feeds output rows hr - 2 .. hr (tap dy = hr - r); their
+// accumulators are adjacent TMEM columns and their weight blocks ([dx][dy = 2, 1, 0])
+// adjacent rows, so one MMA of N = rows x n_tile covers up to STACK of them and the A
+// operand is read once per (hr, dx, kk) instead of once per output row. The loop runs
+// over halo rows outermost, so consecutive MMAs accumulate into the same columns. In a
+// tile's first chunk the row a halo row reaches first (r = hr, at dx = 0, kk = 0) starts
+// its accumulator with a non-accumulating MMA of its own.
+template <int CK, int R, int STACK, bool FIRST>
+__device__ __forceinline__ void halo_chunk_mmas(uint64_t ad0, uint64_t bd0, uint32_t acc, const HaloMmaConsts& k) {
+    constexpr uint32_t W_ROW = CK * 2, HALO_ROW = kHaloW * W_ROW;
+#pragma unroll
+    for (int hr = 0; hr < R + 2; ++hr) {
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+#pragma unroll
+            for (int kk = 0; kk < CK / 16; ++kk) {
+                const uint64_t ad = ad0 + (((uint32_t)hr * HALO_ROW + (uint32_t)dx * W_ROW + kk * 32) >> 4);
+                const int lo = hr - 2 > 0 ? hr - 2 : 0;
+                int hi = hr < R - 1 ? hr : R - 1;
+                if (FIRST && dx == 0 && kk == 0 && hi == hr) {
+                    tc::mma_bf16(acc + k.dcol[hr], ad, bd0 + k.boff[dx * 3 + 2] + kk * 2, k.idesc[0], 0u);
+                    --hi;
+                }
+#pragma unroll
+                for (int r0 = lo; r0 <= hi; r0 += STACK) {
+                    const int r1 = r0 + STACK - 1 < hi ? r0 + STACK - 1 : hi;
+                    tc::mma_bf16(acc + k.dcol[r0], ad, bd0 + k.boff[dx * 3 + 2 - (hr - r0)] + kk * 2,
+                                 k.idesc[r1 - r0], 1u);
+                }
+            }
+        }
+    }
+}
+
+template <int CK, int R, int STACK>
 __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_constant__ CUtensorMap tmX,
                                                                  const __grid_constant__ CUtensorMap tmW,
                                                                  const HaloParams p) {
-    constexpr int G = CK / 8;                          // 16-byte channel groups per chunk
-    constexpr uint32_t W_ROW = CK * 2;                 // bytes per weight row (the swizzle width)
+    constexpr uint32_t W_ROW = CK * 2;                 // bytes per pixel row and weight row (the swizzle width)
     constexpr uint32_t W_LAYOUT = CK == 32 ? 4u : 6u;  // 64 B / 32 B swizzle
-    constexpr uint32_t ROW_BYTES = kHaloW * 16;        // one channel group of one halo row
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* halo = smem;
@@ -327,9 +374,19 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
     if (warp == 0 && lane == 0) {
         // ---- producer ----
         bool ok = true;
+        // the weights of a chunk in shared memory as 9 blocks of n_tile rows in the order
+        // [dx][dy = 2, 1, 0]: the blocks of the taps one halo row and shift give the
+        // output rows r, r + 1, r + 2 (dy = j - r) are adjacent, one stacked B operand
+        auto load_weights = [&](uint8_t* dst, uint64_t* bar, int c) {
+#pragma unroll 1
+            for (int tap = 0; tap < 9; ++tap) {
+                const int blk = (tap % 3) * 3 + (2 - tap / 3);
+                tc::tma_load_3d(dst + (uint32_t)blk * p.n_tile * W_ROW, &tmW, bar, c * CK, n0, tap);
+            }
+        };
         if (p.w_resident) {
             tc::mbar_arrive_expect_tx(wbar, p.w_bytes);
-            tc::tma_load_3d(wst, &tmW, wbar, 0, n0, 0);
+            load_weights(wst, wbar, 0);
         }
         uint32_t it = 0;
         for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
@@ -344,8 +401,8 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                     break;
                 }
                 tc::mbar_arrive_expect_tx(&full[s], p.halo_bytes + (p.w_resident ? 0u : p.w_bytes));
-                tc::tma_load_5d(halo + s * p.halo_stride, &tmX, &full[s], 0, x0 - 1, c * G, y0 - 1, n_img);
-                if (!p.w_resident) tc::tma_load_3d(wst + s * p.w_stride, &tmW, &full[s], c * CK, n0, 0);
+                tc::tma_load_4d(halo + s * p.halo_stride, &tmX, &full[s], c * CK, x0 - 1, y0 - 1, n_img);
+                if (!p.w_resident) load_weights(wst + s * p.w_stride, &full[s], c);
             }
         }
         // drain: every issued copy must have landed before the CTA may exit
@@ -356,8 +413,15 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
         if (p.w_resident && !tc::mbar_wait(wbar, 0, kWaitBudget)) set_error(13);
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
-        const uint32_t idesc = tc::idesc_bf16(128, (uint32_t)p.n_tile);
         const uint32_t halo0 = tc::smem_u32(halo), w0 = tc::smem_u32(wst);
+        // per-CTA constants of the unrolled MMA sequence (halo_chunk_mmas)
+        HaloMmaConsts k;
+#pragma unroll
+        for (int b = 0; b < 9; ++b) k.boff[b] = (uint32_t)(b * p.n_tile) * W_ROW >> 4;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) k.idesc[q] = tc::idesc_bf16(128, (uint32_t)((q + 1) * p.n_tile));
+#pragma unroll
+        for (int r = 0; r < R; ++r) k.dcol[r] = (uint32_t)(r * p.n_tile);
         bool ok = !p.w_resident || tc::mbar_wait(wbar, 0, kWaitBudget);
         if (!ok) set_error(14);
         uint32_t it = 0, j = 0;
@@ -379,21 +443,12 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                 tc::fence_after_sync();
                 const uint32_t ha = halo0 + s * p.halo_stride;
                 const uint32_t wa = w0 + (p.w_resident ? 0u : s * p.w_stride);
-                for (int r = 0; r < p.R; ++r) {
-#pragma unroll
-                    for (int tap = 0; tap < 9; ++tap) {
-                        const uint32_t row = (uint32_t)(r + tap / 3);  // halo row r + dy + 1
-#pragma unroll
-                        for (int kk = 0; kk < CK / 16; ++kk) {
-                            const uint64_t ad = tc::smem_desc_noswz(
-                                ha + (row * G + 2 * kk) * ROW_BYTES + (uint32_t)(tap % 3) * 16u, ROW_BYTES, 128u);
-                            const uint64_t bd = tc::smem_desc(wa + (uint32_t)tap * p.n_tile * W_ROW + kk * 32,
-                                                              8u * W_ROW, W_LAYOUT);
-                            tc::mma_bf16(acc + (uint32_t)(r * p.n_tile), ad, bd, idesc,
-                                         (c > 0 || tap > 0 || kk > 0) ? 1u : 0u);
-                        }
-                    }
-                }
+                const uint64_t ad0 = tc::smem_desc(ha, 8u * W_ROW, W_LAYOUT);
+                const uint64_t bd0 = tc::smem_desc(wa, 8u * W_ROW, W_LAYOUT);
+                if (c == 0)
+                    halo_chunk_mmas<CK, R, STACK, true>(ad0, bd0, acc, k);
+                else
+                    halo_chunk_mmas<CK, R, STACK, false>(ad0, bd0, acc, k);
                 tc::mma_commit(&empty[s]);
             }
             if (!ok) break;
@@ -579,9 +634,13 @@ struct HaloShape {
     size_t smem = 0;
 };
 
+int halo_stack(int n_tile) { return std::min(3, 256 / n_tile); }
+
 bool halo_shape(int Cin, int n_tile, HaloShape& out) {
     for (int R : {4, 2, 1}) {
         if (2 * R * n_tile > 512) continue;
+        const int S = halo_stack(n_tile);
+        if (!((R == 4 && S == 3) || (R == 2 && S >= 2) || (R == 1 && S == 1))) continue;
         for (int CK : {32, 16}) {
             if (Cin % CK) continue;
             HaloShape h;
@@ -610,16 +669,29 @@ int num_sms() {
     return std::max(1, n);
 }
 
-template <int CK> void launch_halo(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p,
-                                   size_t smem, cudaStream_t st) {
+template <int CK, int R, int STACK>
+void launch_halo(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p, size_t smem,
+                 cudaStream_t st) {
     static bool configured = false;
     if (!configured) {
-        KF_CUDA_CHECK(cudaFuncSetAttribute(k_conv_halo<CK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        KF_CUDA_CHECK(cudaFuncSetAttribute(k_conv_halo<CK, R, STACK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            227 * 1024));
         configured = true;
     }
-    k_conv_halo<CK><<<grid, kHaloThreads, smem, st>>>(x, w, p);
+    k_conv_halo<CK, R, STACK><<<grid, kHaloThreads, smem, st>>>(x, w, p);
     KF_CUDA_CHECK(cudaGetLastError());
+}
+
+// One instantiation per (rows per tile, stacked rows): R = 4 comes with n_tile <= 64, so
+// STACK = 3; R = 2 with n_tile <= 128 (STACK 2 or 3); R = 1 with n_tile > 128 (STACK 1).
+// halo_shape takes no other pair.
+template <int CK> void launch_halo_ck(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p,
+                                      size_t smem, cudaStream_t st) {
+    if (p.R == 4 && p.stack == 3) launch_halo<CK, 4, 3>(grid, x, w, p, smem, st);
+    else if (p.R == 2 && p.stack == 2) launch_halo<CK, 2, 2>(grid, x, w, p, smem, st);
+    else if (p.R == 2 && p.stack == 3) launch_halo<CK, 2, 3>(grid, x, w, p, smem, st);
+    else if (p.R == 1 && p.stack == 1) launch_halo<CK, 1, 1>(grid, x, w, p, smem, st);
+    else throw KfError(KF_ERR_INTERNAL, "conv3x3: no halo kernel for this tile shape");
 }
 
 // The halo kernel for images at least one 128-pixel tile wide. Returns 0 when no shape
@@ -630,14 +702,16 @@ int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __n
     const int n_tile = Cout_rows <= 256 ? Cout_rows : 128;
     HaloShape h;
     if (W < 128 || !halo_shape(Cin, n_tile, h)) return 0;
-    // input as [n][y][channel group][x][8 channels]: dims (8, W, Cin / 8, H, N)
-    const uint64_t xdims[5] = {8, (uint64_t)W, (uint64_t)Cin / 8, (uint64_t)H, (uint64_t)N};
-    const uint64_t xstr[4] = {(uint64_t)Cin * 2, 16, (uint64_t)W * Cin * 2, (uint64_t)H * W * Cin * 2};
-    const uint32_t xbox[5] = {8, (uint32_t)kHaloW, (uint32_t)h.CK / 8, (uint32_t)h.R + 2, 1};
-    const CUtensorMap mx = make_map(x, 5, xdims, xstr, xbox, CU_TENSOR_MAP_SWIZZLE_NONE);
+    // input NHWC: dims (Cin, W, H, N), a box of CK channels x 130 pixels x (R + 2) rows,
+    // swizzled like the weights (CK x 2 bytes per row)
+    const uint64_t xdims[4] = {(uint64_t)Cin, (uint64_t)W, (uint64_t)H, (uint64_t)N};
+    const uint64_t xstr[3] = {(uint64_t)Cin * 2, (uint64_t)W * Cin * 2, (uint64_t)H * W * Cin * 2};
+    const uint32_t xbox[4] = {(uint32_t)h.CK, (uint32_t)kHaloW, (uint32_t)h.R + 2, 1};
+    const CUtensorMap mx = make_map(x, 4, xdims, xstr, xbox,
+                                    h.CK == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
     const uint64_t wdims[3] = {(uint64_t)Cin, (uint64_t)Cout_rows, 9};
     const uint64_t wstr[2] = {(uint64_t)Cin * 2, (uint64_t)Cout_rows * Cin * 2};
-    const uint32_t wbox[3] = {(uint32_t)h.CK, (uint32_t)n_tile, 9};
+    const uint32_t wbox[3] = {(uint32_t)h.CK, (uint32_t)n_tile, 1};  // one tap per copy
     const CUtensorMap mw = make_map(w, 3, wdims, wstr, wbox,
                                     h.CK == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
     HaloParams p{};
@@ -649,6 +723,7 @@ int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __n
     p.tiles_y = (H + h.R - 1) / h.R;
     p.num_tiles = p.tiles_x * p.tiles_y * N;
     p.w_resident = h.w_resident ? 1 : 0;
+    p.stack = halo_stack(n_tile);
     p.halo_bytes = h.halo_bytes;
     p.halo_stride = h.halo_stride;
     p.w_bytes = h.w_bytes;
@@ -671,9 +746,9 @@ int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __n
     const int per_slice = std::max(1, num_sms() / slices);
     const dim3 grid((unsigned)std::min(p.num_tiles, per_slice), (unsigned)slices, 1);
     if (h.CK == 32)
-        launch_halo<32>(grid, mx, mw, p, h.smem, st);
+        launch_halo_ck<32>(grid, mx, mw, p, h.smem, st);
     else
-        launch_halo<16>(grid, mx, mw, p, h.smem, st);
+        launch_halo_ck<16>(grid, mx, mw, p, h.smem, st);
     return fused ? 2 : 1;
 }
 

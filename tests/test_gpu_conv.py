@@ -26,11 +26,13 @@ def _tc_error():
     (3, 8, 8, 96, 160, 160, True, 160, 0),
     (1, 33, 17, 32, 288, 288, False, 288, 0),
     # images at least 128 wide: the persistent halo kernel (rows per tile R, channel
-    # chunk CK, resident or streamed weights, ragged last tile in x and y, channel slices)
+    # chunk CK, resident or streamed weights, ragged last tile in x and y, channel slices,
+    # 1 to 3 output rows per MMA)
     (1, 9, 150, 32, 32, 32, False, 96, 32),     # R 4, CK 32, resident weights
     (2, 7, 200, 96, 32, 32, True, 32, 0),       # 3 streamed chunks of 32
     (1, 10, 131, 64, 64, 64, True, 160, 96),    # CK 16, 4 chunks
-    (1, 5, 256, 160, 160, 160, True, 160, 0),   # R 1, n 160
+    (1, 5, 256, 160, 160, 160, True, 160, 0),   # R 1, n 160, one row per MMA
+    (1, 6, 130, 32, 80, 80, True, 80, 0),       # R 2, n 80: three output rows per MMA (N 240)
     (1, 6, 140, 32, 288, 288, False, 288, 0),   # three 128-row slices of the weights
     (2, 3, 128, 64, 40, 48, False, 40, 0),      # N 48, output channels not a multiple of 8
     (1, 13, 384, 96, 224, 224, True, 224, 0),   # no halo shape fits: falls back to the tile kernel
