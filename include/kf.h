@@ -388,6 +388,13 @@ KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d);
  * and its gradients (copied to grads_dev, may be NULL, FP32, num_params) and, if apply,
  * one Adam step with learning rate lr. */
 KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* base, int n, int h, int w, float* out);
+/* The network input of camera c's current frame, as kf_denoiser_apply builds it: BF16
+ * features [hp][wp][32] (g(radiance), albedo, normal, t / (1 + t), log2(samples) / 8, then
+ * zeros) and the FP32 residual base [hp][wp] float4 (g(radiance)), with hp, wp the frame
+ * size rounded up to 16 (padding pixels zero). *hp, *wp are set first; feat_dev and
+ * base_dev (device memory of hp * wp pixels) may be NULL to query the size only. */
+KF_API int kf_denoiser_camera_features(kf_denoiser d, kf_camera c, void* feat_dev, float* base_dev, int* hp,
+                                       int* wp);
 KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* base, const float* target, int n,
                                   int h, int w, float lr, float* grads_dev, int apply, float* loss);
 

@@ -248,6 +248,7 @@ PROTOTYPES = {
     "kf_denoiser_apply": (I, [VP, VP]),
     "kf_renderer_set_denoiser": (I, [VP, VP]),
     "kf_denoiser_forward": (I, [VP, VP, VP, I, I, I, VP]),
+    "kf_denoiser_camera_features": (I, [VP, VP, VP, VP, C.POINTER(I), C.POINTER(I)]),
     "kf_denoiser_train_step": (I, [VP, VP, VP, VP, I, I, I, F, VP, I, C.POINTER(F)]),
 }
 

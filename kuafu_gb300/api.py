@@ -631,6 +631,20 @@ class Denoiser:
     def forward(self, feat_ptr: int, n: int, h: int, w: int, out_ptr: int, base_ptr: int | None = None):
         N.check(_lib().kf_denoiser_forward(self._h, feat_ptr, base_ptr, n, h, w, out_ptr))
 
+    def cameraFeatures(self, cam: Camera):
+        """The network input of cam's current frame: (BF16 features [hp, wp, 32], FP32 base
+        [hp, wp, 4]) as torch CUDA tensors."""
+        import torch
+
+        hp, wp = C.c_int(), C.c_int()
+        N.check(_lib().kf_denoiser_camera_features(self._h, cam._h, None, None, C.byref(hp), C.byref(wp)))
+        feat = torch.empty((hp.value, wp.value, 32), dtype=torch.bfloat16, device="cuda")
+        base = torch.empty((hp.value, wp.value, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        N.check(_lib().kf_denoiser_camera_features(self._h, cam._h, feat.data_ptr(), base.data_ptr(), C.byref(hp),
+                                                   C.byref(wp)))
+        return feat, base
+
     def trainStep(self, feat_ptr: int, target_ptr: int, n: int, h: int, w: int, lr: float = 0.0,
                   grads_ptr: int | None = None, apply: bool = False, base_ptr: int | None = None) -> float:
         loss = C.c_float()

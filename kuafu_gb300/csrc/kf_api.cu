@@ -1430,6 +1430,23 @@ KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* bas
         sync_stream(denoiser_renderer(d));
     });
 }
+KF_API int kf_denoiser_camera_features(kf_denoiser d, kf_camera c, void* feat_dev, float* base_dev, int* hp,
+                                       int* wp) {
+    return guarded([&] {
+        REQ(hp && wp, "null argument");
+        check_denoiser(d);
+        kf_camera_s* cam = check_camera(c);
+        KF_REQUIRE(cam->has_frame, KF_ERR_STATE, "the camera has no frame");
+        *hp = (cam->target_h + 15) / 16 * 16;
+        *wp = (cam->target_w + 15) / 16 * 16;
+        if (!feat_dev && !base_dev) return;
+        REQ(feat_dev && base_dev, "both feature and base buffers are needed");
+        kf_renderer_s* r = denoiser_renderer(d);
+        KF_CUDA_CHECK(cudaSetDevice(r->device));
+        denoiser_camera_features(d, cam, feat_dev, base_dev);
+        sync_stream(r);
+    });
+}
 KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* base, const float* target, int n,
                                   int h, int w, float lr, float* grads_dev, int apply, float* loss) {
     return guarded([&] {

@@ -694,14 +694,16 @@ template <int CK> void launch_halo_ck(dim3 grid, const CUtensorMap& x, const CUt
     else throw KfError(KF_ERR_INTERNAL, "conv3x3: no halo kernel for this tile shape");
 }
 
-// The halo kernel for images at least one 128-pixel tile wide. Returns 0 when no shape
+// The halo kernel for images at least 96 pixels wide. Returns 0 when no shape
 // fits (the caller takes the per-tile kernel), 1 when it ran, 2 when it also did the fused work.
 int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __nv_bfloat16* w, int Cout_rows,
                  const float* bias, int Cout, bool relu, __nv_bfloat16* y, int y_cstride, int y_coff,
                  cudaStream_t st, float* y_f32, const ConvFuse* fuse) {
     const int n_tile = Cout_rows <= 256 ? Cout_rows : 128;
     HaloShape h;
-    if (W < 128 || !halo_shape(Cin, n_tile, h)) return 0;
+    // a tile is 128 pixels of one row: from 96 pixels wide on, at most a quarter of its
+    // rows are padding (the per-tile kernel takes narrower images)
+    if (W < 96 || !halo_shape(Cin, n_tile, h)) return 0;
     // input NHWC: dims (Cin, W, H, N), a box of CK channels x 130 pixels x (R + 2) rows,
     // swizzled like the weights (CK x 2 bytes per row)
     const uint64_t xdims[4] = {(uint64_t)Cin, (uint64_t)W, (uint64_t)H, (uint64_t)N};

@@ -20,6 +20,7 @@
 #include "kf_conv.h"
 #include "kf_denoise.h"
 #include "kf_host.h"
+#include "kf_tone.cuh"
 
 namespace kf {
 
@@ -247,11 +248,7 @@ __global__ void k_pack_layer(const float* __restrict__ W, int cin, int cout, int
     }
 }
 
-// The network works on g(x) = asinh(x / kTone) of linear radiance: g'(x) = 1 / sqrt(x^2 +
-// kTone^2), so errors in g space weigh like the relMSE metric (x - ref)^2 / (ref^2 + 1e-2).
-constexpr float kTone = 0.1f;
-__device__ __forceinline__ float tone(float x) { return asinhf(fmaxf(x, 0.0f) * (1.0f / kTone)); }
-__device__ __forceinline__ float untone(float y) { return kTone * sinhf(fmaxf(y, 0.0f)); }
+// The network works on g(x) = tone(x) of linear radiance (kf_tone.cuh).
 
 // Network input from render targets: g(radiance), albedo (base colour of the first hit of
 // sample 0), normal, hit distance t / (1 + t), log2(samples) / 8; 32 channels, the rest
@@ -903,6 +900,14 @@ float denoiser_train(kf_denoiser_impl* d, uint32_t iters, uint32_t batch, uint32
                                    lr, nullptr, true);
     }
     return iters ? (float)(acc / iters) : 0.0f;
+}
+
+void denoiser_camera_features(kf_denoiser_impl* d, kf_camera_s* c, void* feat, float* base) {
+    kf_renderer_s* r = d->r;
+    const int Hp = (c->target_h + 15) / 16 * 16, Wp = (c->target_w + 15) / 16 * 16;
+    const uint32_t frames = (r->cfg.accumulate_frames && r->frame_count >= 0) ? (uint32_t)r->frame_count + 1u : 1u;
+    camera_features(c, frames * std::max(r->stats.last_spp, 1u), static_cast<bf16*>(feat),
+                    reinterpret_cast<float4*>(base), Hp, Wp, r->stream);
 }
 
 void denoiser_apply(kf_denoiser_impl* d, kf_camera_s* c) {

@@ -28,6 +28,8 @@ void denoiser_forward(kf_denoiser_impl* d, const void* feat, const void* base, i
 float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const void* base, const float* tgt, int n, int h,
                           int w, float lr, float* grads_out, bool apply_update);
 
+// The network input kf_denoiser_apply builds from the camera's current frame (padded to 16).
+void denoiser_camera_features(kf_denoiser_impl* d, kf_camera_s* c, void* feat, float* base);
 // Renders training pairs of a camera: one frame of low_spp[i] samples per input and one
 // target (high_frames x high_spp, FP64 accumulation) that all num_inputs inputs share.
 void denoiser_add_view(kf_denoiser_impl* d, kf_scene_s* s, kf_camera_s* c, const uint32_t* low_spp,

@@ -291,3 +291,34 @@ def test_views_with_shared_targets():
         assert np.isfinite(loss)
         assert _tc_error() == 0
         d.close()
+
+
+def test_apply_matches_forward_of_camera_features():
+    """kf_denoiser_apply on a frame the halo kernel takes (at least 96 wide, not a multiple
+    of 16) equals forward() of the camera's own features (kf_denoiser_camera_features) plus
+    the residual, mapped by g^-1 in torch and cut to the frame (tolerance: torch's sinh
+    against CUDA's sinhf)."""
+    import torch
+
+    h, w = 104, 200  # padded to 112 x 208 inside
+    with api.Kuafu(scenes.cornell_config(spp=4, depth=5)) as r:
+        cam = scenes.cornell(r, w, h)
+        r.run()
+        d = api.Denoiser(r, seed=5)
+        d.apply(cam)
+        assert _tc_error() == 0
+        den = torch.from_numpy(r.downloadAov(cam, N.KF_AOV_DENOISED_F32).copy())
+        feat, base = d.cameraFeatures(cam)
+        hp, wp = feat.shape[:2]
+        assert (hp, wp) == (112, 208)
+        out = torch.empty((hp, wp, 4), device="cuda")
+        torch.cuda.synchronize()
+        d.forward(feat.data_ptr(), 1, hp, wp, out.data_ptr(), base_ptr=base.data_ptr())
+        pred = out[:h, :w, :3].cpu().double()
+        ref = 0.1 * torch.sinh(pred.clamp(min=0.0))
+        got = den[..., :3].double()
+        assert got.shape == ref.shape
+        assert torch.allclose(got, ref, rtol=1e-5, atol=1e-7), (got - ref).abs().max().item()
+        assert (den[..., 3] == 1.0).all()
+        assert ref.abs().max().item() > 0.0
+        d.close()
