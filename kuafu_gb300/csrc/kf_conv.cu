@@ -246,13 +246,14 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 // would read the layer's output again.
 //
 // Warp 0 lane 0: TMA producer (kHaloStages-deep ring). Warp 1 lane 0: MMA issuer.
-// Warps 2-5: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels.
+// Warps 2-9: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels, warps 2-5
+// the first half of the channels and warps 6-9 the second.
 // Every wait is bounded; on expiry the kernel records an error code, lets its own
 // copies and MMAs finish and frees its TMEM.
 // ---------------------------------------------------------------------------
 constexpr int kHaloW = 130;     // 128 output pixels + 2 halo pixels
 constexpr int kHaloStages = 3;
-constexpr int kHaloThreads = 192;
+constexpr int kHaloThreads = 320;  // producer warp, MMA warp, 8 epilogue warps
 
 struct HaloParams {
     int N, H, W, Cin, Cout;
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 4);
+            tc::mbar_init(&acc_empty[b], 8);
         }
         tc::mbar_init(wbar, 1);
         tc::mbar_init(mma_done, 1);
@@ -458,9 +459,11 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
         tc::mma_commit(mma_done);
         if (!tc::mbar_wait(mma_done, 0, kWaitBudget)) set_error(17);
     } else if (warp >= 2) {
-        // ---- epilogue ----
+        // ---- epilogue: 8 warps, two per TMEM lane group, each taking half the channels ----
         const int lg = warp & 3;                 // TMEM lane group of this warp
         const int px_in_tile = lg * 32 + lane;
+        const int half = (warp - 2) >> 2;
+        const int cb = half * (p.n_tile / 2), ce = cb + p.n_tile / 2;  // multiples of 8
         uint32_t j = 0;
         for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++j) {
             const uint32_t b = j & 1;
@@ -501,19 +504,20 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
             if (!p.pool_out) {
                 for (int r = 0; r < p.R; ++r) {
                     const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
-                    for (int c = 0; c < p.n_tile; c += 16) { // two TMEM loads per wait
+                    for (int c = cb; c < ce; c += 16) { // two TMEM loads per wait
                         uint32_t r0[8], r1[8];
+                        const bool two = c + 16 <= ce;
                         tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, r0);
-                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(c + 8), r1);
+                        if (two) tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(c + 8), r1);
                         tc::tmem_ld_wait();
                         float v0[8], v1[8];
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
                             v0[q] = act(r0[q], c + q);
-                            v1[q] = act(r1[q], c + 8 + q);
+                            v1[q] = two ? act(r1[q], c + 8 + q) : 0.0f;
                         }
                         emit8(v0, y0 + r, c);
-                        emit8(v1, y0 + r, c + 8);
+                        if (two) emit8(v1, y0 + r, c + 8);
                     }
                 }
             } else {
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                 for (int r = 0; r < p.R; r += 2) {
                     const int py = y0 + r;
                     const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
-                    for (int c = 0; c < p.n_tile; c += 8) {
+                    for (int c = cb; c < ce; c += 8) {
                         uint32_t ra[8], rc[8];
                         tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, ra);
                         tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(p.n_tile + c), rc);
