@@ -765,7 +765,8 @@ bool conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
                   cudaStream_t st, float* y_f32, const ConvFuse* fuse) {
     KF_REQUIRE(N > 0 && H > 0 && W > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: empty tensor");
     KF_REQUIRE(y || y_f32, KF_ERR_INVALID_ARGUMENT, "conv3x3: no output tensor");
-    KF_REQUIRE(Cin % 32 == 0 && Cin > 0, KF_ERR_INVALID_ARGUMENT, "conv3x3: input channels must be a multiple of 32");
+    KF_REQUIRE((Cin % 32 == 0 && Cin > 0) || Cin == 16, KF_ERR_INVALID_ARGUMENT,
+               "conv3x3: input channels must be 16 or a multiple of 32");
     KF_REQUIRE(Cout > 0 && Cout <= Cout_rows && Cout_rows % 16 == 0, KF_ERR_INVALID_ARGUMENT,
                "conv3x3: weight rows must be a multiple of 16 covering the output channels");
     KF_REQUIRE(y_coff >= 0 && y_coff + Cout <= y_cstride, KF_ERR_INVALID_ARGUMENT, "conv3x3: output slice");
@@ -774,6 +775,8 @@ bool conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     const int halo = conv3x3_halo(x, N, H, W, Cin, w, Cout_rows, bias, Cout, relu, y, y_cstride, y_coff, st, y_f32,
                                   fuse);
     if (halo) return halo == 2;
+    KF_REQUIRE(Cin % 32 == 0, KF_ERR_INVALID_ARGUMENT,
+               "conv3x3: 16 input channels need an image the halo kernel takes (at least 96 wide)");
     // narrow images: one CTA per tile of bw x bh = 128 pixels, 9 tap-shifted boxes per chunk
     int bw = 128;
     while (bw > W && bw > 8) bw >>= 1;

@@ -17,7 +17,8 @@ struct ConvFuse {
 
 // y[n, y, x, y_coff + co] = act(bias[co] + sum_{tap, ci} x[n, y+dy, x+dx, ci] * w[tap][co][ci])
 // NHWC BF16, zero padding, FP32 accumulation on tcgen05. w is [9][Cout_rows][Cin] with
-// Cout_rows a multiple of 16 (rows >= Cout are computed and dropped); Cin % 32 == 0.
+// Cout_rows a multiple of 16 (rows >= Cout are computed and dropped); Cin % 32 == 0, or
+// Cin == 16 for images at least 96 wide.
 // With y_f32 set, the output is written there in FP32 (same strides) and y is unused.
 // Returns true when it also did the fused work asked for in `fuse` (the persistent halo
 // kernel does it for suitable shapes; otherwise the caller runs the separate pass).

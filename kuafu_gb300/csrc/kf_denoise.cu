@@ -248,12 +248,21 @@ __global__ void k_pack_layer(const float* __restrict__ W, int cin, int cout, int
     }
 }
 
+// out[r][c] = in[r][c] for c < cout of rows of cin channels (BF16).
+__global__ void k_slice_cin(const bf16* __restrict__ in, int rows, int cin, int cout, bf16* out) {
+    const size_t total = (size_t)rows * cout;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = in[(i / cout) * cin + i % cout];
+}
+
 // The network works on g(x) = tone(x) of linear radiance (kf_tone.cuh).
 
 // Network input from render targets: g(radiance), albedo (base colour of the first hit of
-// sample 0), normal, hit distance t / (1 + t), log2(samples) / 8; 32 channels, the rest
-// zero. base (optional) receives g(radiance) in FP32: the residual the network corrects.
-// Pixels of the padded tensor outside (H, W) are zero.
+// sample 0), normal, hit distance t / (1 + t), log2(samples) / 8; CH channels (32, or 16
+// for the inference path whose first convolution takes 16), the rest zero. base (optional)
+// receives g(radiance) in FP32: the residual the network corrects. Pixels of the padded
+// tensor outside (H, W) are zero.
+template <int CH>
 __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __restrict__ alb,
                                 const float4* __restrict__ nrm, const float* __restrict__ dep, float spp_feature,
                                 int H, int W, int Hp, int Wp, bf16* out, float4* base) {
@@ -278,9 +287,9 @@ __global__ void k_pack_features(const float4* __restrict__ rad, const float4* __
             f[9] = d / (1.0f + d);
             f[10] = spp_feature;
         }
-        bf16* o = out + i * 32;
+        bf16* o = out + i * CH;
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
+        for (int g = 0; g < CH / 8; ++g) {
             F8 q;
 #pragma unroll
             for (int k = 0; k < 8; ++k) q.v[k] = f[8 * g + k];
@@ -439,6 +448,7 @@ struct kf_denoiser_s {
     size_t nparams = 0, nwf = 0, nwb = 0;
     kf::DeviceBuffer<float> params, grads, m, v;
     kf::DeviceBuffer<__nv_bfloat16> wf, wb;
+    kf::DeviceBuffer<__nv_bfloat16> wf0_16; // first layer, input channels 0..15 (inference)
     kf::DeviceBuffer<float> loss;
     int step = 0;
     bool packed = false;
@@ -520,6 +530,12 @@ void pack(kf_denoiser_impl& d, cudaStream_t st) {
         k_pack_layer<<<grid_for(n), 256, 0, st>>>(d.params.ptr + l.w_off, l.cin, l.cout, l.rows, l.cout_k,
                                                   d.wf.ptr + l.wf_off, d.wb.ptr + l.wb_off);
     }
+    // the first convolution's weights of input channels 0..15 alone: the inference path
+    // feeds it 16-channel features (channels 11..31 of the input are always zero)
+    const Layer& l0 = d.L[0];
+    d.wf0_16.resize((size_t)9 * l0.rows * 16, st);
+    k_slice_cin<<<grid_for((size_t)9 * l0.rows * 16), 256, 0, st>>>(d.wf.ptr + l0.wf_off, 9 * l0.rows, l0.cin, 16,
+                                                                   d.wf0_16.ptr);
     KF_CUDA_CHECK(cudaGetLastError());
     d.packed = true;
 }
@@ -647,10 +663,18 @@ void conv_up(Ctx& c, int li, int level, TRef x, TRef y, TRef up) {
     up_fwd(c, y, level - 1, up);
 }
 
-// prediction (in a.head) = network(T_IN) + base (FP32 residual, optional)
-void forward(Ctx& c, const float4* base) {
+// prediction (in a.head) = network(T_IN) + base (FP32 residual, optional). in16: T_IN holds
+// 16-channel features (the first convolution then reads half the bytes and does half the
+// MMAs; channels 16..31 of the 32-channel input are zero, so the values are the same).
+void forward(Ctx& c, const float4* base, bool in16 = false) {
     Acts& a = c.d.acts;
-    conv_fwd(c, 0, 0, T(a, T_IN), T(a, T_E0A));
+    if (in16) {
+        const Layer& l = c.d.L[0];
+        conv3x3_bf16(a.at(T_IN), c.n, c.h, c.w, 16, c.d.wf0_16.ptr, l.rows, c.d.params.ptr + l.b_off, l.cout, l.relu,
+                     a.at(T_E0A), 32, 0, c.st);
+    } else {
+        conv_fwd(c, 0, 0, T(a, T_IN), T(a, T_E0A));
+    }
     conv_pool(c, 1, 0, T(a, T_E0A), S(a, T_CAT0, 64, 32), T(a, T_P0));
     conv_fwd(c, 2, 1, T(a, T_P0), T(a, T_E1A));
     conv_pool(c, 3, 1, T(a, T_E1A), S(a, T_CAT1, 96, 64), T(a, T_P1));
@@ -797,11 +821,15 @@ float denoiser_train_step(kf_denoiser_impl* d, const void* feat, const void* bas
 
 // Features (and residual base) of a camera's current render targets, padded to [1][Hp][Wp].
 static void camera_features(kf_camera_s* c, uint32_t samples, bf16* out, float4* base, int Hp, int Wp,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool ch16 = false) {
     const float spp_feature = std::log2((float)std::max(samples, 1u)) / 8.0f;
-    k_pack_features<<<grid_for((size_t)Hp * Wp), 256, 0, st>>>(c->accum.ptr, c->albedo.ptr, c->normal.ptr,
-                                                               c->depth.ptr, spp_feature, c->target_h, c->target_w,
-                                                               Hp, Wp, out, base);
+    const unsigned grid = grid_for((size_t)Hp * Wp);
+    if (ch16)
+        k_pack_features<16><<<grid, 256, 0, st>>>(c->accum.ptr, c->albedo.ptr, c->normal.ptr, c->depth.ptr,
+                                                  spp_feature, c->target_h, c->target_w, Hp, Wp, out, base);
+    else
+        k_pack_features<32><<<grid, 256, 0, st>>>(c->accum.ptr, c->albedo.ptr, c->normal.ptr, c->depth.ptr,
+                                                  spp_feature, c->target_h, c->target_w, Hp, Wp, out, base);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -920,9 +948,12 @@ void denoiser_apply(kf_denoiser_impl* d, kf_camera_s* c) {
     const size_t P = (size_t)Hp * Wp;
     if (d->apply_base.count < P) d->apply_base.resize(P, st);
     const uint32_t frames = (r->cfg.accumulate_frames && r->frame_count >= 0) ? (uint32_t)r->frame_count + 1u : 1u;
-    camera_features(c, frames * std::max(r->stats.last_spp, 1u), d->acts.at(T_IN), d->apply_base.ptr, Hp, Wp, st);
+    // frames the halo convolution takes (at least 96 wide) use the 16-channel input
+    const bool in16 = Wp >= 96;
+    camera_features(c, frames * std::max(r->stats.last_spp, 1u), d->acts.at(T_IN), d->apply_base.ptr, Hp, Wp, st,
+                    in16);
     Ctx cx{*d, st, 1, Hp, Wp};
-    forward(cx, d->apply_base.ptr);
+    forward(cx, d->apply_base.ptr, in16);
     const size_t npix = (size_t)c->target_w * c->target_h;
     if (c->denoised.count != npix) c->denoised.resize(npix, st);
     k_unpack<<<grid_for(npix), 256, 0, st>>>(reinterpret_cast<const float4*>(d->acts.head.ptr), c->target_h,

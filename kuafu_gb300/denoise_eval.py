@@ -51,9 +51,12 @@ _LAYERS = [(32, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 96, 2), (96,
 
 
 def unet_flops(h: int, w: int) -> float:
-    """Dense multiply-add FLOPs of one inference (2 * H_l * W_l * Cin * Cout * 9 summed over convs)."""
+    """Dense multiply-add FLOPs one inference executes (2 * H_l * W_l * Cin * Cout * 9 summed
+    over convs). Frames at least 96 wide feed the first convolution 16 input channels (the
+    11 features and 5 zeros) instead of 32."""
     hp, wp = (h + 15) // 16 * 16, (w + 15) // 16 * 16
-    return float(sum(2.0 * (hp >> l) * (wp >> l) * ci * co * 9 for ci, co, l in _LAYERS))
+    layers = [(16, 32, 0)] + _LAYERS[1:] if wp >= 96 else _LAYERS
+    return float(sum(2.0 * (hp >> l) * (wp >> l) * ci * co * 9 for ci, co, l in layers))
 
 
 class _Timer:

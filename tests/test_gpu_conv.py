@@ -33,6 +33,7 @@ def _tc_error():
     (1, 10, 131, 64, 64, 64, True, 160, 96),    # CK 16, 4 chunks
     (1, 5, 256, 160, 160, 160, True, 160, 0),   # R 1, n 160, one row per MMA
     (1, 6, 130, 32, 80, 80, True, 80, 0),       # R 2, n 80: three output rows per MMA (N 240)
+    (1, 9, 140, 16, 32, 32, True, 32, 0),       # 16 input channels (the inference input layer)
     (1, 6, 140, 32, 288, 288, False, 288, 0),   # three 128-row slices of the weights
     (2, 3, 128, 64, 40, 48, False, 40, 0),      # N 48, output channels not a multiple of 8
     (1, 13, 384, 96, 224, 224, True, 224, 0),   # no halo shape fits: falls back to the tile kernel
