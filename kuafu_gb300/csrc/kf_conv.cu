@@ -255,6 +255,26 @@ constexpr int kHaloW = 130;     // 128 output pixels + 2 halo pixels
 constexpr int kHaloStages = 3;
 constexpr int kHaloThreads = 320;  // producer warp, MMA warp, 8 epilogue warps
 
+// 8 or 16 FP32 values stored as BF16 with one 16- or 32-byte store (dst 16- / 32-byte aligned)
+__device__ __forceinline__ void st_bf16x8(__nv_bfloat16* dst, const float (&v)[8]) {
+    __nv_bfloat162 q2[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+    *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(q2);
+}
+__device__ __forceinline__ void st_bf16x16(__nv_bfloat16* dst, const float (&v0)[8], const float (&v1)[8]) {
+    __nv_bfloat162 q2[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        q2[q] = __floats2bfloat162_rn(v0[2 * q], v0[2 * q + 1]);
+        q2[4 + q] = __floats2bfloat162_rn(v1[2 * q], v1[2 * q + 1]);
+    }
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(q2);
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "r"(w[0]), "r"(w[1]),
+                 "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+
 struct HaloParams {
     int N, H, W, Cin, Cout;
     int n_tile, R, kchunks;
@@ -464,6 +484,10 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
         const int px_in_tile = lg * 32 + lane;
         const int half = (warp - 2) >> 2;
         const int cb = half * (p.n_tile / 2), ce = cb + p.n_tile / 2;  // multiples of 8
+        // 32-byte stores need 32-byte aligned rows: the tensor, the channel stride and slice
+        const bool wide = !p.outf && p.out && ((uintptr_t)p.out & 31) == 0 && (p.out_cstride & 15) == 0;
+        const bool pool_wide = p.pool_out && ((uintptr_t)p.pool_out & 31) == 0 && (p.Cout & 15) == 0 &&
+                               (n0 & 15) == 0;
         uint32_t j = 0;
         for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++j) {
             const uint32_t b = j & 1;
@@ -496,6 +520,18 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                 else
                     for (int q = 0; q < 8 && co + q < p.Cout; ++q) dst[q] = __float2bfloat16_rn(v[q]);
             };
+            // 16 channels [cc, cc + 16): one 32-byte store (a whole L2 sector) when aligned
+            auto emit16 = [&](const float(&v0)[8], const float(&v1)[8], int py, int cc) {
+                const int co = n0 + cc;
+                if (wide && co + 16 <= p.Cout && ((p.out_coff + co) & 15) == 0) {
+                    if (!(px < p.W && py < p.H)) return;
+                    const size_t base = ((size_t)((size_t)n_img * p.H + py) * p.W + px) * p.out_cstride + p.out_coff;
+                    st_bf16x16(p.out + base + co, v0, v1);
+                    return;
+                }
+                emit8(v0, py, cc);
+                emit8(v1, py, cc + 8);
+            };
             auto act = [&](uint32_t raw, int cc) {
                 const float v = __uint_as_float(raw) + sbias[cc];
                 return p.relu ? fmaxf(v, 0.0f) : v;
@@ -516,8 +552,10 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                             v0[q] = act(r0[q], c + q);
                             v1[q] = two ? act(r1[q], c + 8 + q) : 0.0f;
                         }
-                        emit8(v0, y0 + r, c);
-                        if (two) emit8(v1, y0 + r, c + 8);
+                        if (two)
+                            emit16(v0, v1, y0 + r, c);
+                        else
+                            emit8(v0, y0 + r, c);
                     }
                 }
             } else {
@@ -528,31 +566,53 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
                 for (int r = 0; r < p.R; r += 2) {
                     const int py = y0 + r;
                     const uint32_t col0 = (b * (uint32_t)p.R + (uint32_t)r) * (uint32_t)p.n_tile;
-                    for (int c = cb; c < ce; c += 8) {
-                        uint32_t ra[8], rc[8];
-                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, ra);
-                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(p.n_tile + c), rc);
+                    for (int c = cb; c < ce; c += 16) {
+                        const bool two = c + 16 <= ce;
+                        uint32_t ra[16], rc[16];
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)c, *reinterpret_cast<uint32_t(*)[8]>(ra));
+                        tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(p.n_tile + c),
+                                     *reinterpret_cast<uint32_t(*)[8]>(rc));
+                        if (two) {
+                            tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(c + 8),
+                                         *reinterpret_cast<uint32_t(*)[8]>(ra + 8));
+                            tc::tmem_ld8(tmem + lanes + col0 + (uint32_t)(p.n_tile + c + 8),
+                                         *reinterpret_cast<uint32_t(*)[8]>(rc + 8));
+                        }
                         tc::tmem_ld_wait();
-                        float va[8], vc[8], pooled[8];
+                        float va[16], vc[16], pooled[16];
 #pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            va[q] = act(ra[q], c + q);
-                            vc[q] = act(rc[q], c + q);
+                        for (int q = 0; q < 16; ++q) {
+                            const bool live = q < 8 || two;
+                            va[q] = live ? act(ra[q], c + q) : 0.0f;
+                            vc[q] = live ? act(rc[q], c + q) : 0.0f;
                             const float a = __bfloat162float(__float2bfloat16_rn(va[q]));
                             const float cv = __bfloat162float(__float2bfloat16_rn(vc[q]));
                             const float bv = __shfl_xor_sync(0xFFFFFFFFu, a, 1);
                             const float dv = __shfl_xor_sync(0xFFFFFFFFu, cv, 1);
                             pooled[q] = 0.25f * (((a + bv) + cv) + dv);
                         }
-                        emit8(va, py, c);
-                        emit8(vc, py + 1, c);
+                        const float(&va0)[8] = *reinterpret_cast<const float(*)[8]>(va);
+                        const float(&va1)[8] = *reinterpret_cast<const float(*)[8]>(va + 8);
+                        const float(&vc0)[8] = *reinterpret_cast<const float(*)[8]>(vc);
+                        const float(&vc1)[8] = *reinterpret_cast<const float(*)[8]>(vc + 8);
+                        if (two) {
+                            emit16(va0, va1, py, c);
+                            emit16(vc0, vc1, py + 1, c);
+                        } else {
+                            emit8(va0, py, c);
+                            emit8(vc0, py + 1, c);
+                        }
                         const int co = n0 + c;
                         if ((lane & 1) == 0 && px + 1 < p.W && py + 1 < p.H && co < p.Cout) {
-                            __nv_bfloat162 q2[4];
-#pragma unroll
-                            for (int q = 0; q < 4; ++q) q2[q] = __floats2bfloat162_rn(pooled[2 * q], pooled[2 * q + 1]);
                             const size_t pb = ((size_t)((size_t)n_img * Hh + py / 2) * Wh + px / 2) * p.Cout + co;
-                            *reinterpret_cast<uint4*>(p.pool_out + pb) = *reinterpret_cast<const uint4*>(q2);
+                            const float(&p0)[8] = *reinterpret_cast<const float(*)[8]>(pooled);
+                            const float(&p1)[8] = *reinterpret_cast<const float(*)[8]>(pooled + 8);
+                            if (two && pool_wide && co + 16 <= p.Cout && (co & 15) == 0)
+                                st_bf16x16(p.pool_out + pb, p0, p1);
+                            else {
+                                st_bf16x8(p.pool_out + pb, p0);
+                                if (two && co + 8 < p.Cout) st_bf16x8(p.pool_out + pb + 8, p1);
+                            }
                         }
                     }
                 }
