@@ -131,6 +131,17 @@ def build_scene(device: int, profile=False, debug=False):
     return r, cam
 
 
+def _per_ray(sc, closest: bool) -> dict:
+    """Node visits, triangle tests and instance entries per ray of one traversal kind
+    (counting variant of the kernels)."""
+    if closest:
+        n = max(sc.rays_primary + sc.rays_extension, 1)
+        return {"node_visits": sc.node_visits / n, "tri_tests": sc.tri_tests / n, "inst_entries": sc.inst_visits / n}
+    n = max(sc.rays_shadow, 1)
+    return {"node_visits": sc.shadow_node_visits / n, "tri_tests": sc.shadow_tri_tests / n,
+            "inst_entries": sc.shadow_inst_visits / n}
+
+
 def separate_blas_summary(device: int, steps: int = 5) -> dict:
     """The same frame with blas_share = 0: every icosphere geometry keeps its own copy of
     the BLAS nodes and triangles (256 copies, ~150 MB against the 129 MB L2) instead of the
@@ -580,6 +591,7 @@ def run_ours(args):
                                             "frac": (achieved / peak) if achieved else None},
                          "bytes_per_ray": (k_bytes / ((sc.rays_primary + sc.rays_extension) if dom_ext else
                                                       max(sc.rays_shadow, 1))),
+                         "per_ray": _per_ray(sc, dom_ext),
                          "kernel_ms_per_frame": {"extend": sp.extend_ms, "shade": sp.shade_ms,
                                                  "shadow": sp.shadow_ms, "frame": sp.frame_ms}},
             "blas": {"shared": {"blas_nodes": shared_nodes,
