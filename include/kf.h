@@ -92,8 +92,8 @@ typedef struct kf_config {
                                       (1..64, default 32) */
     uint32_t blas_share;           /* 1 (default): geometries with identical positions and
                                       indices (materials may differ) share one BLAS in the
-                                      node and triangle pools; 0: one copy per geometry.
-                                      Host SAH builds only. Same hits either way. */
+                                      node and triangle pools, built once; 0: one copy per
+                                      geometry. Same hits either way. */
 } kf_config;
 
 /* Fills kuafu's defaults (config.hpp:140-176). */

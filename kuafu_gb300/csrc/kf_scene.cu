@@ -314,7 +314,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         // the instance names the geometry, so the hit is the same), else each gets its own
         std::vector<size_t> build_of(ng);
         std::vector<size_t> to_build;
-        if (sah) {
+        {
             std::unordered_map<uint64_t, std::vector<size_t>> seen;
             auto fnv = [](uint64_t h, const void* p, size_t n) {
                 const unsigned char* b = static_cast<const unsigned char*>(p);
@@ -412,23 +412,23 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             }
             node_base = (uint32_t)pool.size();
         }
+        // GPU LBVH builds (bvh_builder = 0), one per geometry; with blas_share a geometry
+        // identical to an earlier one takes that one's BLAS instead of a build of its own
         for (size_t gi = 0; gi < ng && !sah; ++gi) {
             const uint32_t ntri = geom[gi].z;
             if (ntri == 0) continue;
-            int nn;
-            if (sah) {
-                nodes.upload(sah_nodes[gi].data(), sah_nodes[gi].size(), st);
-                order.upload(sah_order[gi].data(), sah_order[gi].size(), st);
-                nn = (int)sah_nodes[gi].size();
-            } else {
-                lo.resize(ntri, st);
-                hi.resize(ntri, st);
-                k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, geom[gi].x, geom[gi].y,
-                                                                ntri, lo.ptr, hi.ptr);
-                KF_CUDA_CHECK(cudaGetLastError());
-                nn = build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes, order,
-                                    st);
+            if (r->cfg.blas_share && build_of[gi] != gi) {
+                G.blas_root[gi] = G.blas_root[build_of[gi]];
+                G.blas_box[gi] = G.blas_box[build_of[gi]];
+                continue;
             }
+            lo.resize(ntri, st);
+            hi.resize(ntri, st);
+            k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, geom[gi].x, geom[gi].y, ntri,
+                                                            lo.ptr, hi.ptr);
+            KF_CUDA_CHECK(cudaGetLastError());
+            const int nn =
+                build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes, order, st);
             k_tri_gather<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, order.ptr, geom[gi].x,
                                                              geom[gi].y, ntri, G.tris.ptr + geom[gi].y);
             k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y, 0u,
