@@ -656,8 +656,8 @@ void conv_pool(Ctx& c, int li, int level, TRef x, TRef y, TRef pooled) {
     if (!conv_fwd(c, li, level, x, y, &f)) pool_fwd(c, y, level, pooled);
 }
 // conv into y, then nearest 2x upsampling of y into the channel slice `up` (at level - 1).
-// A separate pass: written from the conv epilogue the four scattered copies per pixel cost
-// more than reading the output once more.
+// A separate pass: both forms are bound by the same HBM writes of the four copies, and
+// written from the conv epilogue (32-byte stores) the layer grew by what the pass takes.
 void conv_up(Ctx& c, int li, int level, TRef x, TRef y, TRef up) {
     conv_fwd(c, li, level, x, y);
     up_fwd(c, y, level - 1, up);
