@@ -538,13 +538,14 @@ def run_ours(args):
         # the traversal's roofline denominator: achievable L2 read bandwidth of this GPU
         l2_peak = rp.measureL2Read()
         rp.close()
-        lbvh_ms = None
-        if WORKLOAD.get("bvh_builder", 1) != 0:
-            WORKLOAD["bvh_builder"] = 0
-            rl, _ = build_scene(device, profile=True)
-            rl.run()
-            lbvh_ms = rl.stats().bvh_build_ms
-            rl.close()
+        gpu_build_ms = {}
+        if WORKLOAD.get("bvh_builder", 1) == 1:
+            for b in (0, 2):  # GPU LBVH, GPU PLOC
+                WORKLOAD["bvh_builder"] = b
+                rl, _ = build_scene(device, profile=True)
+                rl.run()
+                gpu_build_ms[b] = rl.stats().bvh_build_ms
+                rl.close()
             del WORKLOAD["bvh_builder"]
         launches = WORKLOAD["depth"] + 1
         node_b, tri_b, inst_b = 128, 48, 64
@@ -599,7 +600,8 @@ def run_ours(args):
                                         "each) and share one BLAS copy (blas_share = 1, the default)"},
                      "separate": separate},
             "bvh_build_ms": {"default (host binned SAH, 256 BLAS + TLAS)": build_ms,
-                             "gpu_lbvh (256 BLAS + TLAS)": lbvh_ms},
+                             "gpu_lbvh (256 BLAS + TLAS)": gpu_build_ms.get(0),
+                             "gpu_ploc (256 BLAS + TLAS)": gpu_build_ms.get(2)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WORKLOAD["width"] * WORKLOAD["height"] * 4},
@@ -639,7 +641,7 @@ def main():
     ap.add_argument("--no-denoise", action="store_true",
                     help="skip the time-to-relMSE experiment (denoiser training and 1080p evaluation)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 128-view workload")
-    ap.add_argument("--bvh-builder", type=int, default=None, help="0: GPU LBVH, 1: host binned SAH")
+    ap.add_argument("--bvh-builder", type=int, default=None, help="0: GPU LBVH, 1: host binned SAH, 2: GPU PLOC")
     ap.add_argument("--leaf", type=int, default=None, help="BLAS leaf size")
     ap.add_argument("--blas-share", type=int, default=None, help="1: identical geometries share one BLAS (default)")
     ap.add_argument("--dyn", type=int, nargs=2, default=None, metavar=("REFILL_BELOW", "STEPS"),

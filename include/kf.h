@@ -85,7 +85,8 @@ typedef struct kf_config {
     uint32_t traversal;            /* 0: one thread per ray; 1: persistent warps with dynamic
                                       ray fetch (default). Both give identical results. */
     uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order, fastest build); 1: host binned
-                                      SAH (default: fewer node visits per ray). Same hits. */
+                                      SAH (default: fewer node visits per ray); 2: GPU PLOC
+                                      (locally-ordered clustering). Same hits. */
     uint32_t dyn_refill_below;     /* persistent traversal: a warp fetches new rays when fewer
                                       lanes than this are busy (1..32, default 16) */
     uint32_t dyn_steps;            /* ... and runs this many traversal steps between fetches

@@ -13,6 +13,16 @@
 //                              leaves over contiguous primitive ranges)
 // Leaves address contiguous ranges of the Morton-sorted primitive order, so the
 // caller reorders primitive payloads once (triangles / instance ids).
+//
+// Alternative to steps 4-5 (bvh_builder = 2): PLOC, parallel locally-ordered clustering
+// (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume Hierarchy
+// Construction", TVCG 2018). The clusters start as the Morton-sorted primitives; in every
+// round each cluster finds, among the clusters at most `radius` positions away in the
+// array, the one whose merged box has the smallest surface area; pairs that chose each
+// other merge into a new node; the array is compacted in order. Ties are broken by the
+// pair's positions, so the globally best pair always chooses itself and every round
+// merges. The leaves are then numbered in depth-first order, which makes every subtree a
+// contiguous primitive range for step 6.
 #include "kf_bvh.h"
 
 #include <algorithm>
@@ -351,6 +361,75 @@ __global__ void k_identity(uint32_t* order, int n) {
     if (i < n) order[i] = (uint32_t)i;
 }
 
+// ---- PLOC rounds ----
+// nn[i] = the position j != i within `radius` of i whose cluster merged with cl[i] has the
+// smallest surface area (ties: smaller min(i, j), then smaller max(i, j)).
+__global__ void k_ploc_nn(const int* __restrict__ cl, int m, const float4* __restrict__ blo,
+                          const float4* __restrict__ bhi, int radius, int* nn) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int ci = cl[i];
+    const float4 a0 = blo[ci], a1 = bhi[ci];
+    float best = INFINITY;
+    int bj = -1, blo_i = 0x7FFFFFFF, bhi_i = 0x7FFFFFFF;
+    const int j0 = max(0, i - radius), j1 = min(m - 1, i + radius);
+    for (int j = j0; j <= j1; ++j) {
+        if (j == i) continue;
+        const int cj = cl[j];
+        const float4 b0 = blo[cj], b1 = bhi[cj];
+        const float4 lo = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f);
+        const float4 hi = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+        const float sa = surface_area(lo, hi);
+        const int l = min(i, j), h = max(i, j);
+        if (sa < best || (sa == best && (l < blo_i || (l == blo_i && h < bhi_i)))) {
+            best = sa;
+            bj = j;
+            blo_i = l;
+            bhi_i = h;
+        }
+    }
+    nn[i] = bj;
+}
+
+// Mutual nearest neighbours merge: the lower position makes internal node
+// (n - 2 - k) for the k-th merge (the root, made last, gets node 0; children always have
+// larger indices than their parent) and keeps it; the higher one drops out.
+__global__ void k_ploc_merge(int* cl, int m, const int* __restrict__ nn, int n, int* left, int* right, float4* blo,
+                             float4* bhi, int* merges, uint32_t* keep, uint32_t* offs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = nn[i];
+    uint32_t k = 1;
+    if (j >= 0 && nn[j] == i) {
+        if (i < j) {
+            const int id = (n - 2) - atomicAdd(merges, 1);
+            const int a = cl[i], b = cl[j];
+            left[id] = a;
+            right[id] = b;
+            const float4 a0 = blo[a], a1 = bhi[a], b0 = blo[b], b1 = bhi[b];
+            blo[id] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f);
+            bhi[id] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+            cl[i] = id;
+        } else {
+            k = 0;
+        }
+    }
+    keep[i] = k;
+    offs[i] = k;
+}
+
+// cl_out[offs[i]] = cl[i] for the kept clusters (offs: exclusive scan of keep)
+__global__ void k_ploc_compact(const int* __restrict__ cl, int m, const uint32_t* __restrict__ keep,
+                               const uint32_t* __restrict__ offs, int* cl_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m && keep[i]) cl_out[offs[i]] = cl[i];
+}
+
+__global__ void k_iota_leaves(int* cl, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) cl[i] = (n - 1) + i;
+}
+
 } // namespace
 
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* counts,
@@ -378,8 +457,80 @@ size_t radix_sort_count_words(int n) {
     return (size_t)256 * std::max(tiles, 1);
 }
 
+// PLOC binary tree over the n Morton-sorted primitives (order: sorted primitive ids, on
+// return in depth-first leaf order): internal nodes 0..n-2 (root 0), leaf p at (n-1)+p
+// for position p of `order`, range[] the contiguous leaf positions of every internal node,
+// boxes of all 2n-1 nodes in blo / bhi. Same layout as the Karras path.
+static void ploc_tree(const float4* plo, const float4* phi, int n, uint32_t* order, int* left, int* right,
+                      int2* range, float4* blo, float4* bhi, cudaStream_t st) {
+    constexpr int kRadius = 16;
+    const int tb = 256;
+    TempAlloc arena(st);
+    int* cl = arena.alloc<int>(n);
+    int* cl2 = arena.alloc<int>(n);
+    int* nn = arena.alloc<int>(n);
+    uint32_t* keep = arena.alloc<uint32_t>(n);
+    uint32_t* offs = arena.alloc<uint32_t>(n);
+    int* merges = arena.alloc<int>(1);
+    k_leaf_boxes<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, order, n, blo, bhi);
+    k_iota_leaves<<<(n + tb - 1) / tb, tb, 0, st>>>(cl, n);
+    KF_CUDA_CHECK(cudaMemsetAsync(merges, 0, sizeof(int), st));
+    int m = n, rounds = 0;
+    while (m > 1) {
+        KF_REQUIRE(++rounds <= 4 * 32 + 64, KF_ERR_INTERNAL, "PLOC clustering did not converge");
+        const unsigned g = (unsigned)((m + tb - 1) / tb);
+        k_ploc_nn<<<g, tb, 0, st>>>(cl, m, blo, bhi, kRadius, nn);
+        k_ploc_merge<<<g, tb, 0, st>>>(cl, m, nn, n, left, right, blo, bhi, merges, keep, offs);
+        k_sort_scan<<<1, 1024, 0, st>>>(offs, m);
+        k_ploc_compact<<<g, tb, 0, st>>>(cl, m, keep, offs, cl2);
+        KF_CUDA_CHECK(cudaGetLastError());
+        uint32_t last[2];
+        KF_CUDA_CHECK(cudaMemcpyAsync(&last[0], offs + (m - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        KF_CUDA_CHECK(cudaMemcpyAsync(&last[1], keep + (m - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        KF_CUDA_CHECK(cudaStreamSynchronize(st));
+        const int m2 = (int)(last[0] + last[1]);
+        KF_REQUIRE(m2 < m, KF_ERR_INTERNAL, "PLOC round without a merge");
+        m = m2;
+        std::swap(cl, cl2);
+    }
+    // depth-first leaf numbering on the host: leaf counts bottom-up (children have larger
+    // indices than their parent), first positions top-down
+    std::vector<int> hl(n - 1), hr(n - 1);
+    std::vector<uint32_t> ho(n);
+    KF_CUDA_CHECK(cudaMemcpyAsync(hl.data(), left, sizeof(int) * (n - 1), cudaMemcpyDeviceToHost, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(hr.data(), right, sizeof(int) * (n - 1), cudaMemcpyDeviceToHost, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(ho.data(), order, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
+    KF_CUDA_CHECK(cudaStreamSynchronize(st));
+    auto count = [&](int node, const std::vector<int>& cnt) { return node >= n - 1 ? 1 : cnt[node]; };
+    std::vector<int> cnt(n - 1), first(2 * n - 1);
+    for (int id = n - 2; id >= 0; --id) cnt[id] = count(hl[id], cnt) + count(hr[id], cnt);
+    first[0] = 0;
+    for (int id = 0; id < n - 1; ++id) {
+        first[hl[id]] = first[id];
+        first[hr[id]] = first[id] + count(hl[id], cnt);
+    }
+    std::vector<int2> hrange(n - 1);
+    std::vector<uint32_t> new_order(n);
+    auto leaf_id = [&](int node) { return node >= n - 1 ? (n - 1) + first[node] : node; };
+    for (int id = 0; id < n - 1; ++id) {
+        hrange[id] = make_int2(first[id], first[id] + cnt[id] - 1);
+        for (int c : {hl[id], hr[id]})
+            if (c >= n - 1) new_order[first[c]] = ho[c - (n - 1)];
+        hl[id] = leaf_id(hl[id]);
+        hr[id] = leaf_id(hr[id]);
+    }
+    KF_CUDA_CHECK(cudaMemcpyAsync(left, hl.data(), sizeof(int) * (n - 1), cudaMemcpyHostToDevice, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(right, hr.data(), sizeof(int) * (n - 1), cudaMemcpyHostToDevice, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(range, hrange.data(), sizeof(int2) * (n - 1), cudaMemcpyHostToDevice, st));
+    KF_CUDA_CHECK(cudaMemcpyAsync(order, new_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+    // leaf boxes in the new leaf order (the internal boxes are unions of the same leaves)
+    k_leaf_boxes<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, order, n, blo, bhi);
+    KF_CUDA_CHECK(cudaGetLastError());
+    KF_CUDA_CHECK(cudaStreamSynchronize(st)); // the host vectors are freed on return
+}
+
 int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, DeviceBuffer<Node4>& nodes_out,
-                   DeviceBuffer<uint32_t>& order_out, cudaStream_t st) {
+                   DeviceBuffer<uint32_t>& order_out, cudaStream_t st, bool ploc) {
     if (n <= 0) {
         nodes_out.resize(0, st);
         order_out.resize(0, st);
@@ -419,10 +570,14 @@ int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, De
     k_centroid_bounds<<<gb, tb, 0, st>>>(plo, phi, n, bounds);
     k_morton<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, n, bounds, keys, order_out.ptr);
     radix_sort_pairs(keys, order_out.ptr, keys_tmp, vals_tmp, counts, n, 32, st);
-    k_karras<<<(n - 1 + tb - 1) / tb, tb, 0, st>>>(keys, n, left, right, parent, range);
-    k_leaf_boxes<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, order_out.ptr, n, blo, bhi);
-    KF_CUDA_CHECK(cudaMemsetAsync(flags, 0, sizeof(int) * n, st));
-    k_refit<<<(n + tb - 1) / tb, tb, 0, st>>>(n, left, right, parent, blo, bhi, flags);
+    if (!ploc) {
+        k_karras<<<(n - 1 + tb - 1) / tb, tb, 0, st>>>(keys, n, left, right, parent, range);
+        k_leaf_boxes<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, order_out.ptr, n, blo, bhi);
+        KF_CUDA_CHECK(cudaMemsetAsync(flags, 0, sizeof(int) * n, st));
+        k_refit<<<(n + tb - 1) / tb, tb, 0, st>>>(n, left, right, parent, blo, bhi, flags);
+    } else {
+        ploc_tree(plo, phi, n, order_out.ptr, left, right, range, blo, bhi, st);
+    }
 
     // Collapse: frontier starts with the BVH2 root (internal node 0) -> BVH4 node 0.
     // Worst case node count for a 4-wide tree over n leaves is below n.

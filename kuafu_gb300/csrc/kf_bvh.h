@@ -16,8 +16,10 @@ size_t radix_sort_count_words(int n);
 // On return `order` holds the primitive permutation leaves address (leaf child
 // = first position in `order`, cnt = number of consecutive entries) and `nodes`
 // the node pool with the root at index 0. Returns the number of nodes.
+// ploc: the binary tree by locally-ordered clustering over the Morton order (Meister and
+// Bittner 2018) instead of the Karras radix tree; same outputs.
 int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, DeviceBuffer<Node4>& nodes,
-                   DeviceBuffer<uint32_t>& order, cudaStream_t st);
+                   DeviceBuffer<uint32_t>& order, cudaStream_t st, bool ploc = false);
 
 // The same 4-wide layout built on the host by binned SAH (surface area heuristic, 32
 // bins on each axis) and collapsed from the binary tree by opening the child of largest

@@ -412,7 +412,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             }
             node_base = (uint32_t)pool.size();
         }
-        // GPU LBVH builds (bvh_builder = 0), one per geometry; with blas_share a geometry
+        // GPU builds (bvh_builder 0: LBVH, 2: PLOC), one per geometry; with blas_share a geometry
         // identical to an earlier one takes that one's BLAS instead of a build of its own
         for (size_t gi = 0; gi < ng && !sah; ++gi) {
             const uint32_t ntri = geom[gi].z;
@@ -428,7 +428,8 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
                                                             lo.ptr, hi.ptr);
             KF_CUDA_CHECK(cudaGetLastError());
             const int nn =
-                build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes, order, st);
+                build_wide_bvh(lo.ptr, hi.ptr, (int)ntri, (int)std::max(1u, r->cfg.blas_leaf_size), nodes, order, st,
+                               r->cfg.bvh_builder == 2);
             k_tri_gather<<<(ntri + 255) / 256, 256, 0, st>>>(G.verts.ptr, G.indices.ptr, order.ptr, geom[gi].x,
                                                              geom[gi].y, ntri, G.tris.ptr + geom[gi].y);
             k_rebase<<<(nn + 127) / 128, 128, 0, st>>>(nodes.ptr, (uint32_t)nn, node_base, geom[gi].y, 0u,
@@ -623,7 +624,7 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
                 order.upload(ho.data(), ho.size(), st);
             } else {
                 nn = build_wide_bvh(dlo.ptr, dhi.ptr, (int)nv, (int)std::max(1u, r->cfg.tlas_leaf_size),
-                                    G.tlas_nodes, order, st);
+                                    G.tlas_nodes, order, st, r->cfg.bvh_builder == 2);
             }
             G.tlas_inst.resize(nv, st);
             k_map_ids<<<(nv + 255) / 256, 256, 0, st>>>(order.ptr, dids.ptr, nv, G.tlas_inst.ptr);

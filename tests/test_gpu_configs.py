@@ -6,7 +6,7 @@
   from bounce 4, 1 directional + 4 point + 2 spot lights, background 0.1 (the Mrays/s
   workload): the GPU renders the whole frame, the oracle traverses its own CPU BVH for
   fixed crops of it (deep BLAS, long traversal stacks, 9-trace paths).
-* Both BVH builders (GPU LBVH and host binned SAH) give the same hits and paths.
+* All three BVH builders (GPU LBVH, host binned SAH, GPU PLOC) give the same hits and paths.
 * Converged FP64 accumulation: the GPU's FP64 sum of 1024 spp against the oracle's FP64
   render, on the same sample streams (agreement far below the noise) and on independent
   streams (agreement within the noise floor of 1024 spp).
@@ -118,10 +118,11 @@ def test_icospheres_full_scene_ray_count(c2_frame):
     assert ext > 0.3 * prim and shadow > prim
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 @pytest.mark.parametrize("leaf", [1, 4, 16])
 def test_both_bvh_builders_find_the_same_hits(builder, leaf):
-    """GPU LBVH (bvh_builder 0) and host binned SAH (1) change the tree, never the hits."""
+    """GPU LBVH (bvh_builder 0), host binned SAH (1) and GPU PLOC (2) change the tree, never
+    the hits."""
     spp, depth = 2, 3
     cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
     cfg.setDebugOutputs(True)
@@ -146,23 +147,27 @@ def test_both_bvh_builders_find_the_same_hits(builder, leaf):
     assert within >= MIN_WITHIN
 
 
-def test_gpu_lbvh_on_the_full_icosphere_scene():
-    """The GPU LBVH builds the 256 BLAS of the 1.31 M-triangle scene; its hits equal the
-    host SAH tree's over the whole 1080p frame."""
+@pytest.mark.parametrize("share", [1, 0])
+def test_gpu_builders_on_the_full_icosphere_scene(share):
+    """The GPU LBVH and PLOC builders build the 1.31 M-triangle scene (one shared BLAS, or
+    256 separate builds); their hits equal the host SAH tree's over the whole 1080p frame."""
     res = []
-    for builder in (0, 1):
+    for builder in (0, 2, 1):
         cfg = scenes.icosphere_config(spp=1, depth=1, count=256)
         cfg.setDebugOutputs(True)
         cfg.setBvhBuilder(builder)
+        cfg.setBlasShare(share)
         with api.Kuafu(cfg) as r:
             cam = scenes.icospheres(r, 1920, 1080, count=256, level=4, seed=0)
             r.run()
             res.append(r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, 1))
-    assert np.array_equal(res[0]["instance"], res[1]["instance"])
-    hit = res[0]["instance"] != 0xFFFFFFFF
+    ref = res[-1]
+    hit = ref["instance"] != 0xFFFFFFFF
     assert hit.mean() > 0.2
-    assert np.array_equal(res[0]["prim"][hit], res[1]["prim"][hit])
-    assert np.array_equal(res[0]["t"][hit], res[1]["t"][hit])
+    for got in res[:-1]:
+        assert np.array_equal(got["instance"], ref["instance"])
+        assert np.array_equal(got["prim"][hit], ref["prim"][hit])
+        assert np.array_equal(got["t"][hit], ref["t"][hit])
 
 
 def test_shared_blas_gives_the_same_frame():
