@@ -26,6 +26,7 @@
 #include "kf_bvh.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <vector>
 
@@ -611,9 +612,11 @@ int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, De
 }
 
 // ---------------------------------------------------------------------------
-// Host binned-SAH builder (Wald 2007, "On fast construction of SAH-based bounding
-// volume hierarchies": 32 bins per axis over the centroid bounds, cost = C_node +
-// sum_i SA_i / SA * N_i), then the 4-wide collapse of the binary tree.
+// Host SAH builder (cost = C_node + sum_i SA_i / SA * N_i): nodes of at most kSweepMax
+// primitives try every split of the centroid-sorted order on each axis (a full sweep);
+// larger nodes take 32 bins per axis over the centroid bounds (Wald 2007, "On fast
+// construction of SAH-based bounding volume hierarchies"). Then the 4-wide collapse of the
+// binary tree.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -644,6 +647,8 @@ struct BNode {
     int first, count;
 };
 
+constexpr int kSweepMax = 4096;
+
 struct SahBuilder {
     const float* lo;
     const float* hi;
@@ -651,6 +656,46 @@ struct SahBuilder {
     std::vector<uint32_t> idx;
     std::vector<float> cen; // 3 per primitive
     std::vector<BNode> nodes;
+    std::vector<uint32_t> sweep_order[3]; // scratch of the full sweep (consumed before recursing)
+    std::vector<float> sweep_area;
+
+    // Best SAH split of idx[begin, end) over all centroid-sorted orders: on success the range
+    // is left in the winning axis's order and the split position is returned, else -1.
+    int sweep_split(int begin, int end) {
+        const int n = end - begin;
+        float best_cost = INFINITY;
+        int best_axis = -1, best_at = 0;
+        sweep_area.resize(n);
+        for (int axis = 0; axis < 3; ++axis) {
+            std::vector<uint32_t>& o = sweep_order[axis];
+            o.assign(idx.begin() + begin, idx.begin() + end);
+            std::sort(o.begin(), o.end(), [&](uint32_t a, uint32_t b) {
+                const float ca = cen[3 * a + axis], cb = cen[3 * b + axis];
+                return ca < cb || (ca == cb && a < b);
+            });
+            HBox acc;
+            acc.reset();
+            for (int i = n - 1; i > 0; --i) {
+                acc.grow(prim_box(o[i]));
+                sweep_area[i] = acc.area();
+            }
+            acc.reset();
+            for (int i = 0; i < n - 1; ++i) {
+                acc.grow(prim_box(o[i]));
+                const float cost = acc.area() * (float)(i + 1) + sweep_area[i + 1] * (float)(n - i - 1);
+                // equal costs (coincident boxes): the split nearest the middle
+                if (cost < best_cost ||
+                    (cost == best_cost && std::abs(2 * (i + 1) - n) < std::abs(2 * best_at - n))) {
+                    best_cost = cost;
+                    best_axis = axis;
+                    best_at = i + 1;
+                }
+            }
+        }
+        if (best_axis < 0) return -1;
+        std::copy(sweep_order[best_axis].begin(), sweep_order[best_axis].end(), idx.begin() + begin);
+        return begin + best_at;
+    }
 
     HBox prim_box(uint32_t p) const {
         HBox b;
@@ -677,6 +722,14 @@ struct SahBuilder {
         const int n = end - begin;
         if (n <= max_leaf) { // leaves never exceed max_leaf (traversal encodes <= 16 triangles)
             nodes[node] = BNode{box, -1, -1, begin, n};
+            return node;
+        }
+        if (n <= kSweepMax && depth < 48) {
+            int mid = sweep_split(begin, end);
+            if (mid <= begin || mid >= end) mid = begin + n / 2;
+            const int l = build(begin, mid, depth + 1);
+            const int r = build(mid, end, depth + 1);
+            nodes[node] = BNode{box, l, r, begin, n};
             return node;
         }
         constexpr int kBins = 32;
