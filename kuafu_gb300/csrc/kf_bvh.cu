@@ -364,7 +364,10 @@ __global__ void k_identity(uint32_t* order, int n) {
 
 // ---- PLOC rounds ----
 // nn[i] = the position j != i within `radius` of i whose cluster merged with cl[i] has the
-// smallest surface area (ties: smaller min(i, j), then smaller max(i, j)).
+// smallest surface area. Ties (coincident boxes) go to the nearer position, then to the
+// pair starting at an even position, then to the lower pair: a total order on pairs that
+// both ends share, so the best pair always chooses itself, and runs of equal clusters pair
+// off as (2k, 2k + 1) and halve in one round.
 __global__ void k_ploc_nn(const int* __restrict__ cl, int m, const float4* __restrict__ blo,
                           const float4* __restrict__ bhi, int radius, int* nn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -372,7 +375,7 @@ __global__ void k_ploc_nn(const int* __restrict__ cl, int m, const float4* __res
     const int ci = cl[i];
     const float4 a0 = blo[ci], a1 = bhi[ci];
     float best = INFINITY;
-    int bj = -1, blo_i = 0x7FFFFFFF, bhi_i = 0x7FFFFFFF;
+    int bj = -1, bd = 0x7FFFFFFF, bodd = 2, bl = 0x7FFFFFFF;
     const int j0 = max(0, i - radius), j1 = min(m - 1, i + radius);
     for (int j = j0; j <= j1; ++j) {
         if (j == i) continue;
@@ -381,15 +384,25 @@ __global__ void k_ploc_nn(const int* __restrict__ cl, int m, const float4* __res
         const float4 lo = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f);
         const float4 hi = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
         const float sa = surface_area(lo, hi);
-        const int l = min(i, j), h = max(i, j);
-        if (sa < best || (sa == best && (l < blo_i || (l == blo_i && h < bhi_i)))) {
+        const int l = min(i, j), d = abs(i - j), odd = l & 1;
+        if (sa < best ||
+            (sa == best && (d < bd || (d == bd && (odd < bodd || (odd == bodd && l < bl)))))) {
             best = sa;
             bj = j;
-            blo_i = l;
-            bhi_i = h;
+            bd = d;
+            bodd = odd;
+            bl = l;
         }
     }
     nn[i] = bj;
+}
+
+// Fallback rounds (inputs on which the greedy rounds stall): neighbours (2k, 2k + 1) pair up.
+__global__ void k_ploc_pairs(int m, int* nn) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = i ^ 1;
+    nn[i] = j < m ? j : -1;
 }
 
 // Mutual nearest neighbours merge: the lower position makes internal node
@@ -476,11 +489,17 @@ static void ploc_tree(const float4* plo, const float4* phi, int n, uint32_t* ord
     k_leaf_boxes<<<(n + tb - 1) / tb, tb, 0, st>>>(plo, phi, order, n, blo, bhi);
     k_iota_leaves<<<(n + tb - 1) / tb, tb, 0, st>>>(cl, n);
     KF_CUDA_CHECK(cudaMemsetAsync(merges, 0, sizeof(int), st));
+    // greedy rounds reduce the clusters by about a third each; after kGreedyRounds the
+    // rest pair up in order, which halves them every round and ends on any input
+    constexpr int kGreedyRounds = 64;
     int m = n, rounds = 0;
     while (m > 1) {
-        KF_REQUIRE(++rounds <= 4 * 32 + 64, KF_ERR_INTERNAL, "PLOC clustering did not converge");
+        KF_REQUIRE(++rounds <= kGreedyRounds + 40, KF_ERR_INTERNAL, "PLOC clustering did not converge");
         const unsigned g = (unsigned)((m + tb - 1) / tb);
-        k_ploc_nn<<<g, tb, 0, st>>>(cl, m, blo, bhi, kRadius, nn);
+        if (rounds <= kGreedyRounds)
+            k_ploc_nn<<<g, tb, 0, st>>>(cl, m, blo, bhi, kRadius, nn);
+        else
+            k_ploc_pairs<<<g, tb, 0, st>>>(m, nn);
         k_ploc_merge<<<g, tb, 0, st>>>(cl, m, nn, n, left, right, blo, bhi, merges, keep, offs);
         k_sort_scan<<<1, 1024, 0, st>>>(offs, m);
         k_ploc_compact<<<g, tb, 0, st>>>(cl, m, keep, offs, cl2);

@@ -263,3 +263,54 @@ def test_1080p_reference_crop_against_fp64_oracle():
     print(f"1080p reference crop: relMSE vs FP64 oracle {got:.3e}, expected noise {expected:.3e}")
     assert c > 0
     assert got < 2.0 * expected
+
+
+@pytest.mark.parametrize("builder", [0, 1, 2])
+def test_builders_with_coincident_triangles(builder):
+    """Degenerate input for every builder: 200 copies of one triangle, 100 copies of another
+    and a strip of distinct ones, in one geometry (equal Morton codes, equal split and merge
+    costs). The hits equal the oracle's brute force, the lowest primitive winning a tie."""
+    rng = np.random.default_rng(5)
+    pos, idx = [], []
+
+    def tri(a, b, c, copies):
+        for _ in range(copies):
+            base = len(pos)
+            pos.extend([a, b, c])
+            idx.extend([base, base + 1, base + 2])
+
+    tri((1.0, -0.8, -0.8), (1.0, 0.8, -0.8), (1.0, 0.0, 0.8), 200)
+    tri((0.5, -0.3, -0.3), (0.5, 0.3, -0.3), (0.5, 0.0, 0.3), 100)
+    for k in range(64):
+        y = -1.0 + k / 32.0
+        z = rng.uniform(-0.5, 0.5)
+        tri((1.5, y, z - 0.5), (1.5, y + 0.03, z - 0.5), (1.5, y, z + 0.5), 1)
+    spp, depth, w, h = 1, 1, 48, 48
+    cfg = scenes.cornell_config(spp=spp, depth=depth)
+    cfg.setDebugOutputs(True)
+    cfg.setBvhBuilder(builder)
+    with api.Kuafu(cfg) as r:
+        s = r.getScene()
+        g = api.Geometry.from_arrays(pos, idx)
+        g.setMaterial(api.NiceMaterial(diffuseColor=(0.7, 0.7, 0.7)))
+        s.submitGeometry(g)
+        s.submitGeometryInstance(api.instance(g, np.eye(4)))
+        cam = s.createCamera(w, h)
+        s.setCamera(cam)
+        cam.setPosition((-2.0, 0.0, 0.0))
+        cam.setFront((1.0, 0.0, 0.0))
+        cam.setUp((0.0, 0.0, 1.0))
+        scenes.pinhole(cam, w, h, 60.0)
+        r.run()
+        hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)
+        ref = O.render(s.export(), cam.ubo(), w, h, O.push_constants(spp, depth), seed=0, frame=0, camera_index=1)
+    rh = ref["hits"]
+    assert np.array_equal(hits["instance"], rh["instance"])
+    hit = rh["instance"] != 0xFFFFFFFF
+    assert hit.mean() > 0.05
+    assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
+    assert np.array_equal(hits["t"][hit], rh["t"][hit])
+    # within each stack of copies the lowest primitive (0, 200) wins every tie
+    p = hits["prim"][hit]
+    assert (p == 200).any() and (p == 0).any()
+    assert not ((p > 0) & (p < 200)).any() and not ((p > 200) & (p < 300)).any()
