@@ -901,7 +901,7 @@ __global__ void __launch_bounds__(kMissThreads) k_miss(SceneDev s, const FrameDe
     }
 }
 
-// Blocks of the shading kernels (k_shade, k_nee): their block scans keep one count per warp.
+// Blocks of the shading kernels (k_shade, k_nee); k_shade's block scan keeps one count per warp.
 constexpr uint32_t kShadeThreads = 128, kShadeWarps = kShadeThreads / 32;
 
 template <bool BATCH>
@@ -1156,10 +1156,8 @@ template <bool BATCH>
 __global__ void __launch_bounds__(kShadeThreads) k_nee(SceneDev s, const FrameDev* __restrict__ fp, BatchDev b, WaveDev w,
                                              uint32_t depth, uint64_t chunk_start) {
     const uint32_t count = w.counters[5];
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
-    __shared__ uint32_t s_cnt[2][kShadeWarps], s_base[2]; // per slot parity: the block scan of emitted rays
-    uint32_t par = 0;
     for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < count; bbase += stride) {
         const uint32_t base = bbase + (threadIdx.x & ~31u);
         const bool valid = base + lane < count;
@@ -1205,24 +1203,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_nee(SceneDev s, const FrameDe
             else
                 emit = is_mat && light_sample(s, SceneLights{s}, j, depth, pk, worldPos, N, V, sh, Ls, tmax, c);
             // each light slot has its own shadow queue, so a shadow-traversal warp takes rays
-            // towards one light from neighbouring points
-            uint32_t pos;
-            if (BATCH) { // slot counts differ between the warps of a block
-                pos = warp_append(emit, &w.scount[j]);
-            } else {
-                const uint32_t m = __ballot_sync(kFull, emit);
-                if (lane == 0) s_cnt[par][wid] = __popc(m);
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    uint32_t t = 0;
-            for (uint32_t k = 0; k < kShadeWarps; ++k) t += s_cnt[par][k];
-                    s_base[par] = t ? atomicAdd(&w.scount[j], t) : 0u;
-                }
-                __syncthreads();
-                pos = s_base[par] + __popc(m & lanemask_lt());
-                for (uint32_t k = 0; k < wid; ++k) pos += s_cnt[par][k];
-                par ^= 1;
-            }
+            // towards one light from neighbouring points; one atomic per warp and slot (a
+            // block-wide scan instead waited at two barriers per slot for the warp with the
+            // longest light sampling)
+            const uint32_t pos = warp_append(emit, &w.scount[j]);
             if (emit) {
                 const size_t q = (size_t)j * w.chunk_cap + pos;
                 w.sq_o[q] = make_float4(worldPos.x, worldPos.y, worldPos.z, tmax);
