@@ -21,10 +21,11 @@ size_t radix_sort_count_words(int n);
 int build_wide_bvh(const float4* plo, const float4* phi, int n, int max_leaf, DeviceBuffer<Node4>& nodes,
                    DeviceBuffer<uint32_t>& order, cudaStream_t st, bool ploc = false);
 
-// The same 4-wide layout built on the host by binned SAH (surface area heuristic, 32
-// bins on each axis) and collapsed from the binary tree by opening the child of largest
-// surface area: usually fewer node visits per ray than the Morton-order build, at host
-// build cost. lo / hi: n x 3 floats. Returns the number of nodes (root at 0).
+// The same 4-wide layout built on the host by SAH (surface area heuristic: every split of
+// the sorted centroids for nodes of up to 4096 primitives, 32 bins per axis above) and
+// collapsed from the binary tree with each node's children chosen by SAH cost: fewer node
+// visits per ray than the Morton-order builds, at host build cost. lo / hi: n x 3 floats.
+// Returns the number of nodes (root at 0).
 int build_wide_bvh_sah_host(const float* lo, const float* hi, int n, int max_leaf, std::vector<Node4>& nodes,
                             std::vector<uint32_t>& order);
 
