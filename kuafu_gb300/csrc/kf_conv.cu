@@ -245,14 +245,16 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 // paired inside a tile, the right neighbour is the next lane), saving the pass that
 // would read the layer's output again.
 //
-// Warp 0 lane 0: TMA producer (kHaloStages-deep ring). Warp 1 lane 0: MMA issuer.
+// Warp 0 lane 0: TMA producer (a ring of halo_stages(R) stages). Warp 1 lane 0: MMA issuer.
 // Warps 2-9: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels, warps 2-5
 // the first half of the channels and warps 6-9 the second.
 // Every wait is bounded; on expiry the kernel records an error code, lets its own
 // copies and MMAs finish and frees its TMEM.
 // ---------------------------------------------------------------------------
 constexpr int kHaloW = 130;     // 128 output pixels + 2 halo pixels
-constexpr int kHaloStages = 3;
+// Halo stages in flight: 3, or 2 for 8-row tiles (whose halo of 10 rows leaves no room
+// for a third in 227 KB).
+__host__ __device__ constexpr int halo_stages(int R) { return R == 8 ? 2 : 3; }
 constexpr int kHaloThreads = 320;  // producer warp, MMA warp, 8 epilogue warps
 
 // 8 or 16 FP32 values stored as BF16 with one 16- or 32-byte store (dst 16- / 32-byte aligned)
@@ -300,7 +302,7 @@ struct HaloParams {
 struct HaloMmaConsts {
     uint32_t boff[9];
     uint32_t idesc[3];
-    uint32_t dcol[4];
+    uint32_t dcol[8];
 };
 
 // The MMAs of one chunk, unrolled at compile time (the single issuing thread then spends a
@@ -343,16 +345,17 @@ template <int CK, int R, int STACK>
 __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_constant__ CUtensorMap tmX,
                                                                  const __grid_constant__ CUtensorMap tmW,
                                                                  const HaloParams p) {
+    constexpr int STAGES = halo_stages(R);
     constexpr uint32_t W_ROW = CK * 2;                 // bytes per pixel row and weight row (the swizzle width)
     constexpr uint32_t W_LAYOUT = CK == 32 ? 4u : 6u;  // 64 B / 32 B swizzle
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* halo = smem;
-    uint8_t* wst = halo + kHaloStages * p.halo_stride;
-    const int w_slots = p.w_resident ? 1 : kHaloStages;
+    uint8_t* wst = halo + STAGES * p.halo_stride;
+    const int w_slots = p.w_resident ? 1 : STAGES;
     uint64_t* full = reinterpret_cast<uint64_t*>(wst + w_slots * p.w_stride);
-    uint64_t* empty = full + kHaloStages;
-    uint64_t* acc_full = empty + kHaloStages;
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;
     uint64_t* acc_empty = acc_full + 2;
     uint64_t* wbar = acc_empty + 2;
     uint64_t* mma_done = wbar + 1;
@@ -367,7 +370,7 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
     for (int i = threadIdx.x; i < p.n_tile; i += blockDim.x)
         sbias[i] = (p.bias && n0 + i < p.Cout) ? p.bias[n0 + i] : 0.0f;
     if (threadIdx.x == 32) {
-        for (int s = 0; s < kHaloStages; ++s) {
+        for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
@@ -414,9 +417,9 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
             int n_img, y0, x0;
             tile_origin(t, n_img, y0, x0);
             for (int c = 0; c < p.kchunks; ++c, ++it) {
-                const uint32_t s = it % kHaloStages;
-                if (it >= (uint32_t)kHaloStages &&
-                    !tc::mbar_wait(&empty[s], ((it / kHaloStages) - 1) & 1, kWaitBudget)) {
+                const uint32_t s = it % STAGES;
+                if (it >= (uint32_t)STAGES &&
+                    !tc::mbar_wait(&empty[s], ((it / STAGES) - 1) & 1, kWaitBudget)) {
                     set_error(11);
                     ok = false;
                     break;
@@ -427,9 +430,9 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
             }
         }
         // drain: every issued copy must have landed before the CTA may exit
-        for (uint32_t s = 0; s < (uint32_t)kHaloStages && s < it; ++s) {
-            const uint32_t last = ((it - 1 - s) / kHaloStages) * kHaloStages + s;
-            if (!tc::mbar_wait(&full[s], (last / kHaloStages) & 1, kWaitBudget)) set_error(12);
+        for (uint32_t s = 0; s < (uint32_t)STAGES && s < it; ++s) {
+            const uint32_t last = ((it - 1 - s) / STAGES) * STAGES + s;
+            if (!tc::mbar_wait(&full[s], (last / STAGES) & 1, kWaitBudget)) set_error(12);
         }
         if (p.w_resident && !tc::mbar_wait(wbar, 0, kWaitBudget)) set_error(13);
     } else if (warp == 1 && lane == 0) {
@@ -455,8 +458,8 @@ __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_cons
             tc::fence_after_sync();
             const uint32_t acc = tmem + b * (uint32_t)acc_cols;
             for (int c = 0; c < p.kchunks; ++c, ++it) {
-                const uint32_t s = it % kHaloStages;
-                if (!tc::mbar_wait(&full[s], (it / kHaloStages) & 1, kWaitBudget)) {
+                const uint32_t s = it % STAGES;
+                if (!tc::mbar_wait(&full[s], (it / STAGES) & 1, kWaitBudget)) {
                     set_error(16);
                     ok = false;
                     break;
@@ -701,10 +704,10 @@ struct HaloShape {
 int halo_stack(int n_tile) { return std::min(3, 256 / n_tile); }
 
 bool halo_shape(int Cin, int n_tile, HaloShape& out) {
-    for (int R : {4, 2, 1}) {
+    for (int R : {8, 4, 2, 1}) {
         if (2 * R * n_tile > 512) continue;
         const int S = halo_stack(n_tile);
-        if (!((R == 4 && S == 3) || (R == 2 && S >= 2) || (R == 1 && S == 1))) continue;
+        if (!((R >= 4 && S == 3) || (R == 2 && S >= 2) || (R == 1 && S == 1))) continue;
         for (int CK : {32, 16}) {
             if (Cin % CK) continue;
             HaloShape h;
@@ -715,8 +718,9 @@ bool halo_shape(int Cin, int n_tile, HaloShape& out) {
             h.halo_stride = (h.halo_bytes + 1023u) & ~1023u;
             h.w_bytes = (uint32_t)(9 * n_tile * CK * 2);
             h.w_stride = (h.w_bytes + 1023u) & ~1023u;
-            h.smem = 1024 + (size_t)kHaloStages * h.halo_stride +
-                     (size_t)(h.w_resident ? 1 : kHaloStages) * h.w_stride + 256 + 4u * (size_t)n_tile;
+            const int stages = halo_stages(R);
+            h.smem = 1024 + (size_t)stages * h.halo_stride +
+                     (size_t)(h.w_resident ? 1 : stages) * h.w_stride + 256 + 4u * (size_t)n_tile;
             if (h.smem <= 227u * 1024u) {
                 out = h;
                 return true;
@@ -746,12 +750,14 @@ void launch_halo(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const Ha
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
-// One instantiation per (rows per tile, stacked rows): R = 4 comes with n_tile <= 64, so
-// STACK = 3; R = 2 with n_tile <= 128 (STACK 2 or 3); R = 1 with n_tile > 128 (STACK 1).
+// One instantiation per (rows per tile, stacked rows): R = 8 comes with n_tile <= 32 and
+// R = 4 with n_tile <= 64, so STACK = 3; R = 2 with n_tile <= 128 (STACK 2 or 3); R = 1
+// with n_tile > 128 (STACK 1).
 // halo_shape takes no other pair.
 template <int CK> void launch_halo_ck(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p,
                                       size_t smem, cudaStream_t st) {
-    if (p.R == 4 && p.stack == 3) launch_halo<CK, 4, 3>(grid, x, w, p, smem, st);
+    if (p.R == 8 && p.stack == 3) launch_halo<CK, 8, 3>(grid, x, w, p, smem, st);
+    else if (p.R == 4 && p.stack == 3) launch_halo<CK, 4, 3>(grid, x, w, p, smem, st);
     else if (p.R == 2 && p.stack == 2) launch_halo<CK, 2, 2>(grid, x, w, p, smem, st);
     else if (p.R == 2 && p.stack == 3) launch_halo<CK, 2, 3>(grid, x, w, p, smem, st);
     else if (p.R == 1 && p.stack == 1) launch_halo<CK, 1, 1>(grid, x, w, p, smem, st);
