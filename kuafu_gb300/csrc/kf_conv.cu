@@ -245,16 +245,15 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 // paired inside a tile, the right neighbour is the next lane), saving the pass that
 // would read the layer's output again.
 //
-// Warp 0 lane 0: TMA producer (a ring of halo_stages(R) stages). Warp 1 lane 0: MMA issuer.
+// Warp 0 lane 0: TMA producer (a ring of STAGES stages). Warp 1 lane 0: MMA issuer.
 // Warps 2-9: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels, warps 2-5
 // the first half of the channels and warps 6-9 the second.
 // Every wait is bounded; on expiry the kernel records an error code, lets its own
 // copies and MMAs finish and frees its TMEM.
 // ---------------------------------------------------------------------------
 constexpr int kHaloW = 130;     // 128 output pixels + 2 halo pixels
-// Halo stages in flight: 3, or 2 for 8-row tiles (whose halo of 10 rows leaves no room
-// for a third in 227 KB).
-__host__ __device__ constexpr int halo_stages(int R) { return R == 8 ? 2 : 3; }
+// Halo stages in flight (STAGES): 3, or 2 where a third does not fit 227 KB (8-row
+// tiles, or 32-channel chunks with streamed weights).
 constexpr int kHaloThreads = 320;  // producer warp, MMA warp, 8 epilogue warps
 
 // 8 or 16 FP32 values stored as BF16 with one 16- or 32-byte store (dst 16- / 32-byte aligned)
@@ -341,11 +340,10 @@ __device__ __forceinline__ void halo_chunk_mmas(uint64_t ad0, uint64_t bd0, uint
     }
 }
 
-template <int CK, int R, int STACK>
+template <int CK, int R, int STACK, int STAGES>
 __global__ void __launch_bounds__(kHaloThreads, 1) k_conv_halo(const __grid_constant__ CUtensorMap tmX,
                                                                  const __grid_constant__ CUtensorMap tmW,
                                                                  const HaloParams p) {
-    constexpr int STAGES = halo_stages(R);
     constexpr uint32_t W_ROW = CK * 2;                 // bytes per pixel row and weight row (the swizzle width)
     constexpr uint32_t W_LAYOUT = CK == 32 ? 4u : 6u;  // 64 B / 32 B swizzle
     extern __shared__ uint8_t smem_raw[];
@@ -695,7 +693,7 @@ void launch_tc(dim3 grid, const CUtensorMap& a, const CUtensorMap& b, const TcPa
 // shared memory it takes. Larger R first (less halo per output row, fewer weight
 // reloads per pixel), then larger CK; both accumulators must fit the 512 TMEM columns.
 struct HaloShape {
-    int R = 0, CK = 0;
+    int R = 0, CK = 0, stages = 3;
     bool w_resident = false;
     uint32_t halo_bytes = 0, halo_stride = 0, w_bytes = 0, w_stride = 0;
     size_t smem = 0;
@@ -708,17 +706,20 @@ bool halo_shape(int Cin, int n_tile, HaloShape& out) {
         if (2 * R * n_tile > 512) continue;
         const int S = halo_stack(n_tile);
         if (!((R >= 4 && S == 3) || (R == 2 && S >= 2) || (R == 1 && S == 1))) continue;
-        for (int CK : {32, 16}) {
+        // 32-channel chunks first (64-byte TMA pieces, half the chunk round trips), with three
+        // stages or, where those do not fit, two; then 16-channel chunks
+        for (const auto [CK, stages] : {std::pair{32, 3}, std::pair{32, 2}, std::pair{16, 3}, std::pair{16, 2}}) {
             if (Cin % CK) continue;
+            if (R == 8 && stages == 3) continue; // an 8-row halo leaves room for two
             HaloShape h;
             h.R = R;
             h.CK = CK;
+            h.stages = stages;
             h.w_resident = Cin == CK;
             h.halo_bytes = (uint32_t)((R + 2) * kHaloW * CK * 2);
             h.halo_stride = (h.halo_bytes + 1023u) & ~1023u;
             h.w_bytes = (uint32_t)(9 * n_tile * CK * 2);
             h.w_stride = (h.w_bytes + 1023u) & ~1023u;
-            const int stages = halo_stages(R);
             h.smem = 1024 + (size_t)stages * h.halo_stride +
                      (size_t)(h.w_resident ? 1 : stages) * h.w_stride + 256 + 4u * (size_t)n_tile;
             if (h.smem <= 227u * 1024u) {
@@ -737,31 +738,38 @@ int num_sms() {
     return std::max(1, n);
 }
 
-template <int CK, int R, int STACK>
+template <int CK, int R, int STACK, int STAGES>
 void launch_halo(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p, size_t smem,
                  cudaStream_t st) {
     static bool configured = false;
     if (!configured) {
-        KF_CUDA_CHECK(cudaFuncSetAttribute(k_conv_halo<CK, R, STACK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           227 * 1024));
+        KF_CUDA_CHECK(cudaFuncSetAttribute(k_conv_halo<CK, R, STACK, STAGES>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         configured = true;
     }
-    k_conv_halo<CK, R, STACK><<<grid, kHaloThreads, smem, st>>>(x, w, p);
+    k_conv_halo<CK, R, STACK, STAGES><<<grid, kHaloThreads, smem, st>>>(x, w, p);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
-// One instantiation per (rows per tile, stacked rows): R = 8 comes with n_tile <= 32 and
-// R = 4 with n_tile <= 64, so STACK = 3; R = 2 with n_tile <= 128 (STACK 2 or 3); R = 1
-// with n_tile > 128 (STACK 1).
-// halo_shape takes no other pair.
+// One instantiation per (rows per tile, stacked rows, stages): R = 8 comes with n_tile <= 32
+// and R = 4 with n_tile <= 64, so STACK = 3; R = 2 with n_tile <= 128 (STACK 2 or 3); R = 1
+// with n_tile > 128 (STACK 1). halo_shape takes no other pair.
+template <int CK, int STAGES>
+bool launch_halo_stages(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p, size_t smem,
+                        cudaStream_t st) {
+    if (p.R == 8 && p.stack == 3 && STAGES == 2) launch_halo<CK, 8, 3, 2>(grid, x, w, p, smem, st);
+    else if (p.R == 4 && p.stack == 3) launch_halo<CK, 4, 3, STAGES>(grid, x, w, p, smem, st);
+    else if (p.R == 2 && p.stack == 2) launch_halo<CK, 2, 2, STAGES>(grid, x, w, p, smem, st);
+    else if (p.R == 2 && p.stack == 3) launch_halo<CK, 2, 3, STAGES>(grid, x, w, p, smem, st);
+    else if (p.R == 1 && p.stack == 1) launch_halo<CK, 1, 1, STAGES>(grid, x, w, p, smem, st);
+    else return false;
+    return true;
+}
 template <int CK> void launch_halo_ck(dim3 grid, const CUtensorMap& x, const CUtensorMap& w, const HaloParams& p,
-                                      size_t smem, cudaStream_t st) {
-    if (p.R == 8 && p.stack == 3) launch_halo<CK, 8, 3>(grid, x, w, p, smem, st);
-    else if (p.R == 4 && p.stack == 3) launch_halo<CK, 4, 3>(grid, x, w, p, smem, st);
-    else if (p.R == 2 && p.stack == 2) launch_halo<CK, 2, 2>(grid, x, w, p, smem, st);
-    else if (p.R == 2 && p.stack == 3) launch_halo<CK, 2, 3>(grid, x, w, p, smem, st);
-    else if (p.R == 1 && p.stack == 1) launch_halo<CK, 1, 1>(grid, x, w, p, smem, st);
-    else throw KfError(KF_ERR_INTERNAL, "conv3x3: no halo kernel for this tile shape");
+                                      int stages, size_t smem, cudaStream_t st) {
+    const bool ok = stages == 2 ? launch_halo_stages<CK, 2>(grid, x, w, p, smem, st)
+                                : launch_halo_stages<CK, 3>(grid, x, w, p, smem, st);
+    if (!ok) throw KfError(KF_ERR_INTERNAL, "conv3x3: no halo kernel for this tile shape");
 }
 
 // The halo kernel for images at least 96 pixels wide. Returns 0 when no shape
@@ -818,9 +826,9 @@ int conv3x3_halo(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __n
     const int per_slice = std::max(1, num_sms() / slices);
     const dim3 grid((unsigned)std::min(p.num_tiles, per_slice), (unsigned)slices, 1);
     if (h.CK == 32)
-        launch_halo_ck<32>(grid, mx, mw, p, h.smem, st);
+        launch_halo_ck<32>(grid, mx, mw, p, h.stages, h.smem, st);
     else
-        launch_halo_ck<16>(grid, mx, mw, p, h.smem, st);
+        launch_halo_ck<16>(grid, mx, mw, p, h.stages, h.smem, st);
     return fused ? 2 : 1;
 }
 
