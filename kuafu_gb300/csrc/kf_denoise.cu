@@ -311,15 +311,19 @@ __global__ void k_add_base(float4* __restrict__ head, const float4* __restrict__
     }
 }
 
-// denoised linear radiance = g^-1(prediction) for the (H, W) window of the padded output
-__global__ void k_unpack(const float4* __restrict__ pred, int H, int W, int Wp, float4* out) {
+// denoised linear radiance = g^-1(prediction + g(radiance)) for the (H, W) window: the
+// residual add and the unpack in one pass, g(radiance) recomputed from the render target
+// (the same function of the same value the feature pass applies, so the same bits)
+__global__ void k_unpack_residual(const float4* __restrict__ pred, const float4* __restrict__ rad, int H, int W,
+                                  int Wp, float4* out) {
     const size_t total = (size_t)H * W;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % W), y = (int)(i / W);
-        const float4 p = pred[(size_t)y * Wp + x];
-        out[i] = make_float4(untone(p.x), untone(p.y), untone(p.z), 1.0f);
+        const float4 p = pred[(size_t)y * Wp + x], r = rad[i];
+        out[i] = make_float4(untone(p.x + tone(r.x)), untone(p.y + tone(r.y)), untone(p.z + tone(r.z)), 1.0f);
     }
 }
+
 
 // L = mean|p - t| + lambda * mean(|dx p - dx t| + |dy p - dy t|) in g space, p the FP32
 // prediction [P][4], t = g(target); writes dL/dp as the BF16 [P][32] gradient of the head.
@@ -462,7 +466,6 @@ struct kf_denoiser_s {
     kf::DeviceBuffer<float4> ds_base, ds_tgt;
     kf::DeviceBuffer<__nv_bfloat16> batch_feat;
     kf::DeviceBuffer<float4> batch_base, batch_tgt;
-    kf::DeviceBuffer<float4> apply_base; // residual base of an inference frame
     kf::DeviceBuffer<int4> crops;
     std::mt19937 rng{1234};
 };
@@ -945,19 +948,16 @@ void denoiser_apply(kf_denoiser_impl* d, kf_camera_s* c) {
     const int Hp = (c->target_h + 15) / 16 * 16, Wp = (c->target_w + 15) / 16 * 16;
     ensure_acts(*d, 1, Hp, Wp, st);
     if (!d->packed) pack(*d, st);
-    const size_t P = (size_t)Hp * Wp;
-    if (d->apply_base.count < P) d->apply_base.resize(P, st);
     const uint32_t frames = (r->cfg.accumulate_frames && r->frame_count >= 0) ? (uint32_t)r->frame_count + 1u : 1u;
     // frames the halo convolution takes (at least 96 wide) use the 16-channel input
     const bool in16 = Wp >= 96;
-    camera_features(c, frames * std::max(r->stats.last_spp, 1u), d->acts.at(T_IN), d->apply_base.ptr, Hp, Wp, st,
-                    in16);
+    camera_features(c, frames * std::max(r->stats.last_spp, 1u), d->acts.at(T_IN), nullptr, Hp, Wp, st, in16);
     Ctx cx{*d, st, 1, Hp, Wp};
-    forward(cx, d->apply_base.ptr, in16);
+    forward(cx, nullptr, in16);
     const size_t npix = (size_t)c->target_w * c->target_h;
     if (c->denoised.count != npix) c->denoised.resize(npix, st);
-    k_unpack<<<grid_for(npix), 256, 0, st>>>(reinterpret_cast<const float4*>(d->acts.head.ptr), c->target_h,
-                                             c->target_w, Wp, c->denoised.ptr);
+    k_unpack_residual<<<grid_for(npix), 256, 0, st>>>(reinterpret_cast<const float4*>(d->acts.head.ptr),
+                                                      c->accum.ptr, c->target_h, c->target_w, Wp, c->denoised.ptr);
     KF_CUDA_CHECK(cudaGetLastError());
 }
 
