@@ -1376,6 +1376,7 @@ KF_API int kf_denoiser_add_view_inputs(kf_denoiser d, kf_scene s, kf_camera c, c
         kf_scene_s* sc = check_scene(s);
         kf_camera_s* cam = check_camera(c);
         REQ(cam->scene == sc, "the camera does not belong to the scene");
+        REQ(sc->renderer == denoiser_renderer(d), "the scene belongs to another renderer");
         REQ(low_spp && num_inputs >= 1 && num_inputs <= 64, "between 1 and 64 inputs per view");
         for (uint32_t i = 0; i < num_inputs; ++i) REQ(low_spp[i] > 0, "sample counts must be positive");
         REQ(high_spp > 0 && high_frames > 0, "sample counts must be positive");
@@ -1410,6 +1411,7 @@ KF_API int kf_denoiser_apply(kf_denoiser d, kf_camera c) {
         check_denoiser(d);
         kf_camera_s* cam = check_camera(c);
         kf_renderer_s* r = denoiser_renderer(d);
+        REQ(cam->scene && cam->scene->renderer == r, "the camera belongs to another renderer");
         KF_CUDA_CHECK(cudaSetDevice(r->device));
         denoiser_apply(d, cam);
         sync_stream(r);
@@ -1436,6 +1438,7 @@ KF_API int kf_denoiser_camera_features(kf_denoiser d, kf_camera c, void* feat_de
         REQ(hp && wp, "null argument");
         check_denoiser(d);
         kf_camera_s* cam = check_camera(c);
+        REQ(cam->scene && cam->scene->renderer == denoiser_renderer(d), "the camera belongs to another renderer");
         KF_REQUIRE(cam->has_frame, KF_ERR_STATE, "the camera has no frame");
         *hp = (cam->target_h + 15) / 16 * 16;
         *wp = (cam->target_w + 15) / 16 * 16;

@@ -322,3 +322,18 @@ def test_apply_matches_forward_of_camera_features():
         assert (den[..., 3] == 1.0).all()
         assert ref.abs().max().item() > 0.0
         d.close()
+
+
+def test_denoiser_refuses_another_renderers_camera():
+    """A denoiser works on its own renderer's cameras and scenes only."""
+    with api.Kuafu(scenes.cornell_config(spp=1, depth=2)) as r1, api.Kuafu(scenes.cornell_config(spp=1, depth=2)) as r2:
+        cam2 = scenes.cornell(r2, 32, 32)
+        r2.run()
+        d = api.Denoiser(r1, seed=0)
+        with pytest.raises(N.KfError):
+            d.apply(cam2)
+        with pytest.raises(N.KfError):
+            d.cameraFeatures(cam2)
+        with pytest.raises(N.KfError):
+            d.addViewInputs(r2.getScene(), cam2, [1], 4, 1)
+        d.close()
