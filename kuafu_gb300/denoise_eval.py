@@ -208,7 +208,7 @@ def _time_to(plain, den, thresholds):
 
 def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_spp=8, plain_checkpoint_step=2048,
         plain_max_spp=65536, train_views=66, train_size=256, train_high_spp=64,
-        train_high_frames=64, train_iters=4000, train_batch=8, train_crop=128, lr=1e-3,
+        train_high_frames=64, train_iters=6000, train_batch=12, train_crop=128, lr=1e-3,
         denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3),
         depth=5, shipped=None, save_trained=None, log=print) -> dict:
     cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
@@ -263,7 +263,8 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
         #    the width x height view
         d = api.Denoiser(r, seed=0)
         t_data = add_training_views(r, cfg, d, train_views, train_size, width, height,
-                                    lambda v: [denoise_spps[v % len(denoise_spps)]], train_high_spp,
+                                    lambda v: [denoise_spps[v % len(denoise_spps)],
+                                               denoise_spps[(v + 5) % len(denoise_spps)]], train_high_spp,
                                     train_high_frames)
         t0 = time.perf_counter()
         losses = _train(r, d, train_iters, train_batch, train_crop, lr)
