@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 }
 
 // ---------------------------------------------------------------------------
-// Halo convolution: persistent, warp-specialised, for images at least one tile wide.
+// Halo convolution: persistent, warp-specialised, for images at least 96 pixels wide.
 //
 // A tile is R output rows x 128 pixels x n_tile output channels: R accumulators of
 // n_tile TMEM columns, double-buffered so the epilogue of one tile overlaps the MMAs of
@@ -237,13 +237,14 @@ __global__ void __launch_bounds__(128, 1) k_tc(const __grid_constant__ CUtensorM
 // the swizzle to the absolute shared-memory address, as TMA does when it writes a box at
 // a 1024-byte aligned address, so a view starting at any row reads the rows TMA wrote
 // (the descriptor's base-offset field stays 0). The halo is read from L2 once per chunk
-// and used by all 9 taps (the per-tap kernel above reads 9 shifted boxes). The weights of a chunk
-// ([tap][n_tile][CK], swizzled rows of CK channels) stream with the halo by TMA, or,
-// when one chunk covers all input channels, are loaded once per CTA.
+// and used by all 9 taps (the per-tap kernel above reads 9 shifted boxes). The weights of a
+// chunk (9 blocks of n_tile rows of CK channels, swizzled, ordered [dx][dy = 2, 1, 0] so
+// that one MMA covers up to STACK output rows: halo_chunk_mmas) stream with the halo by TMA,
+// or, when one chunk covers all input channels, are loaded once per CTA.
 //
-// The epilogue can also do the 2x2 average pooling that follows some layers (rows are
-// paired inside a tile, the right neighbour is the next lane), saving the pass that
-// would read the layer's output again.
+// The epilogue writes 16 channels of a pixel with one 32-byte store and can also do the
+// 2x2 average pooling that follows some layers (rows are paired inside a tile, the right
+// neighbour is the next lane), saving the pass that would read the layer's output again.
 //
 // Warp 0 lane 0: TMA producer (a ring of STAGES stages). Warp 1 lane 0: MMA issuer.
 // Warps 2-9: epilogue, warp w owning TMEM lanes [32 (w % 4), +32) = tile pixels, warps 2-5
