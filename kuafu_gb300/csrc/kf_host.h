@@ -87,7 +87,7 @@ struct SceneGpu {
     uint64_t built_env_version = 0;
     std::vector<uint32_t> blas_root;                 // per geometry
     std::vector<std::array<float, 6>> blas_box;      // per geometry object-space box
-    std::vector<std::vector<float>> blas_hull;      // per geometry: xyz points bounding its triangles
+    std::vector<std::array<double, 10>> blas_bound; // per geometry: vertex box and bounding sphere
     std::vector<uint32_t> tri_offset, vert_offset;   // per geometry
     uint64_t built_geom_stamp = 0;
     uint32_t built_bvh_key = 0;  // builder, leaf size and sharing the BLAS were built with

@@ -102,42 +102,36 @@ __global__ void k_map_ids(const uint32_t* __restrict__ order, const uint32_t* __
     if (i < n) out[i] = ids[order[i]];
 }
 
-// Object-space points whose transformed axis-aligned box contains the geometry's triangles
-// under any affine transform (an instance's world box for the TLAS): the referenced
-// vertices themselves, whose convex hull holds every triangle, up to kHullExact of them;
-// beyond that the 8 corners of the boxes of kHullChunks runs of consecutive referenced
-// vertices. A rotated instance's box from its vertices is tight, where the 8 corners of
-// its object-space box give a box up to sqrt(3) times wider per axis.
-constexpr size_t kHullExact = 16384, kHullChunks = 2048;
-void hull_points(const kf_geometry_s* g, std::vector<float>& out) {
+// Object-space bounds of a geometry's triangles for its instances' world boxes (the TLAS
+// leaf boxes): the box of the referenced vertices, lo[3] hi[3], and the sphere around the
+// box centre through the farthest vertex, centre[3] radius. Both hold every triangle (the
+// convex hull of its vertices), so an instance's world box can be the overlap of the
+// transformed box's box and the transformed sphere's box: O(1) per instance and update, and
+// for a rotated sphere-like mesh as tight as the box of its transformed vertices, where the
+// transformed box corners alone give a box up to sqrt(3) times wider per axis.
+std::array<double, 10> geometry_bound(const kf_geometry_s* g) {
     const size_t nv = g->vertices.size(), ni = g->indices.size() / 3 * 3;
-    std::vector<uint8_t> used(nv, 0);
-    for (size_t i = 0; i < ni; ++i)
-        if (g->indices[i] < nv) used[g->indices[i]] = 1;
-    std::vector<uint32_t> ref;
-    for (size_t v = 0; v < nv; ++v)
-        if (used[v]) ref.push_back((uint32_t)v);
-    out.clear();
-    if (ref.size() <= kHullExact) {
-        out.reserve(ref.size() * 3);
-        for (uint32_t v : ref) out.insert(out.end(), g->vertices[v].pos, g->vertices[v].pos + 3);
-        return;
-    }
-    const size_t per = (ref.size() + kHullChunks - 1) / kHullChunks;
-    out.reserve(kHullChunks * 24);
-    for (size_t c0 = 0; c0 < ref.size(); c0 += per) {
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (size_t j = c0; j < std::min(ref.size(), c0 + per); ++j)
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = std::min(lo[k], g->vertices[ref[j]].pos[k]);
-                hi[k] = std::max(hi[k], g->vertices[ref[j]].pos[k]);
-            }
-        for (int c = 0; c < 8; ++c) {
-            out.push_back((c & 1) ? hi[0] : lo[0]);
-            out.push_back((c & 2) ? hi[1] : lo[1]);
-            out.push_back((c & 4) ? hi[2] : lo[2]);
+    std::array<double, 10> b{INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0, 0, 0, 0};
+    for (size_t i = 0; i < ni; ++i) {
+        if (g->indices[i] >= nv) continue;
+        const float* p = g->vertices[g->indices[i]].pos;
+        for (int k = 0; k < 3; ++k) {
+            b[k] = std::min(b[k], (double)p[k]);
+            b[3 + k] = std::max(b[3 + k], (double)p[k]);
         }
     }
+    if (!(b[0] <= b[3])) return b; // no triangle: the instance is hidden
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) b[6 + k] = 0.5 * (b[k] + b[3 + k]);
+    for (size_t i = 0; i < ni; ++i) {
+        if (g->indices[i] >= nv) continue;
+        const float* p = g->vertices[g->indices[i]].pos;
+        double d2 = 0.0;
+        for (int k = 0; k < 3; ++k) d2 += ((double)p[k] - b[6 + k]) * ((double)p[k] - b[6 + k]);
+        r2 = std::max(r2, d2);
+    }
+    b[9] = std::sqrt(r2);
+    return b;
 }
 
 void root_box(const Node4& n, std::array<float, 6>& b) {
@@ -294,8 +288,8 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         std::vector<Node4> pool_host; // not used: pools are assembled on device
         G.blas_root.assign(ng, 0);
         G.blas_box.assign(ng, {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY});
-        G.blas_hull.assign(ng, {});
-        for (size_t gi = 0; gi < ng; ++gi) hull_points(s->geometries[gi], G.blas_hull[gi]);
+        G.blas_bound.resize(ng);
+        for (size_t gi = 0; gi < ng; ++gi) G.blas_bound[gi] = geometry_bound(s->geometries[gi]);
         size_t total_nodes_est = 0;
         for (size_t gi = 0; gi < ng; ++gi) total_nodes_est += std::max<size_t>(1, s->geometries[gi]->indices.size() / 3);
         G.blas_nodes.resize(std::max<size_t>(total_nodes_est, 1), st);
@@ -516,18 +510,27 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             rc.flags = (g->opaque ? 1u : 0u) | (hidden ? 2u : 0u);
             rc.pad = 0;
             if (hidden) continue;
-            // world box of the transformed hull points (double), padded
-            const std::vector<float>& hp = G.blas_hull[gi];
+            // world box (double, padded): the transformed object box's box overlapped with the
+            // transformed bounding sphere's box (half extent along axis k: radius x |row k|)
+            const std::array<double, 10>& gb = G.blas_bound[gi];
             double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
             const float* m = in->transform;
-            for (size_t c = 0; c + 2 < hp.size(); c += 3) {
-                const double p[3] = {hp[c], hp[c + 1], hp[c + 2]};
+            for (int c = 0; c < 8; ++c) {
+                const double p[3] = {(c & 1) ? gb[3] : gb[0], (c & 2) ? gb[4] : gb[1], (c & 4) ? gb[5] : gb[2]};
                 for (int k = 0; k < 3; ++k) {
                     const double v = (double)m[0 * 4 + k] * p[0] + (double)m[1 * 4 + k] * p[1] +
                                      (double)m[2 * 4 + k] * p[2] + (double)m[3 * 4 + k];
                     mn[k] = std::min(mn[k], v);
                     mx[k] = std::max(mx[k], v);
                 }
+            }
+            for (int k = 0; k < 3; ++k) {
+                const double c = (double)m[0 * 4 + k] * gb[6] + (double)m[1 * 4 + k] * gb[7] +
+                                 (double)m[2 * 4 + k] * gb[8] + (double)m[3 * 4 + k];
+                const double row = std::sqrt((double)m[0 * 4 + k] * m[0 * 4 + k] + (double)m[1 * 4 + k] * m[1 * 4 + k] +
+                                             (double)m[2 * 4 + k] * m[2 * 4 + k]);
+                mn[k] = std::max(mn[k], c - gb[9] * row);
+                mx[k] = std::min(mx[k], c + gb[9] * row);
             }
             double mag = 0.0;
             for (int k = 0; k < 3; ++k) mag = std::max(mag, std::max(std::fabs(mn[k]), std::fabs(mx[k])));
