@@ -18,7 +18,8 @@ at 1920x1080, path depth 5, no Russian roulette. The experiment, all on one GPU:
    1..1024 spp, targets at 4096 spp), then applied to single frames of k spp of the
    held-out scene; time = render + denoise (CUDA events). With `shipped` set, the
    network shipped with the package (train_network: 2000 windows, 4-spp inputs plus
-   one more input per window, 4096-spp targets) is evaluated on the same frames.
+   one more input per window, 4096-spp targets) is evaluated on the same frames, and
+   so is each network of `more_networks` (name -> parameter file).
 4. For each threshold tau: the measured time plain accumulation needs to reach raw
    relMSE <= tau and the time the denoised form needs (smallest k whose denoised
    frame reaches tau), and their ratio. "Debiased" values (raw minus ref_floor)
@@ -29,6 +30,8 @@ in FP64 on the GPU (kf_relmse).
 
   python -m kuafu_gb300.denoise_eval [--small] [--json out.json]
   python -m kuafu_gb300.denoise_eval --train-network kuafu_gb300/weights/unet_cornell_2000x256.kfw
+  python -m kuafu_gb300.denoise_eval --train-network kuafu_gb300/weights/unet_mixed_1500x256.kfw \
+      --views 1200 --icosphere-views 300 --train-iters 8000
 """
 from __future__ import annotations
 
@@ -149,6 +152,37 @@ def add_training_views(r: api.Kuafu, cfg: api.Config, d: api.Denoiser, count: in
     return time.perf_counter() - t0
 
 
+def add_icosphere_views(r: api.Kuafu, cfg: api.Config, d: api.Denoiser, count: int, size: int, full_w: int,
+                        full_h: int, inputs_of, high_spp: int, high_frames: int, spheres: int = 256, log=None) -> float:
+    """Adds `count` training views of icosphere scenes (scenes.icospheres with `spheres`
+    level-4 spheres, seed 20000 + v: placements, materials and lights vary) through
+    size x size windows of their full_w x full_h 60-degree view, rendered at depth 8 with
+    Russian roulette as the icosphere workload is; each scene is removed once its pairs are
+    stored. Returns the seconds taken."""
+    rng = scenes.SplitMix64(0x1C05F00D)
+    t0 = time.perf_counter()
+    cfg.setPathDepth(8)
+    cfg.setRussianRoulette(True)
+    try:
+        for v in range(count):
+            s = r.createScene()
+            c = scenes.icospheres(r, size, size, count=spheres, level=4, seed=20000 + v, scene=s)
+            x0 = min(full_w - size, int(rng.uniform() * (full_w - size + 1)))
+            y0 = min(full_h - size, int(rng.uniform() * (full_h - size + 1)))
+            window_camera(c, size, full_w, full_h, x0, y0, fov_deg=60.0)
+            cfg.setSeed(70000 + v)
+            r.applyConfig()
+            d.addViewInputs(s, c, inputs_of(v), high_spp, high_frames)
+            r.removeScene(s)
+            if log and (v + 1) % 100 == 0:
+                log(f"icosphere views: {v + 1} of {count} ({time.perf_counter() - t0:.0f} s)")
+    finally:
+        cfg.setPathDepth(5)
+        cfg.setRussianRoulette(False)
+        r.applyConfig()
+    return time.perf_counter() - t0
+
+
 def _train(r: api.Kuafu, d: api.Denoiser, iters: int, batch: int, crop: int, lr: float) -> list:
     """Adam over random crops; lr x 0.1 for the last 20 % of the steps. Mean loss per tenth."""
     losses, done, chunk = [], 0, max(1, iters // 10)
@@ -210,7 +244,7 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
         plain_max_spp=65536, train_views=66, train_size=256, train_high_spp=64,
         train_high_frames=64, train_iters=6000, train_batch=12, train_crop=128, lr=1e-3,
         denoise_spps=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3),
-        depth=5, shipped=None, save_trained=None, log=print) -> dict:
+        depth=5, shipped=None, save_trained=None, more_networks=None, log=print) -> dict:
     cfg = scenes.cornell_config(spp=ref_frame_spp, depth=depth)
     res = {"scene": "cornell", "width": width, "height": height, "depth": depth, "eps": EPS}
     with api.Kuafu(cfg) as r:
@@ -294,6 +328,14 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
             res["shipped"] = {"weights": str(shipped), "denoised": den2,
                               "time_to_relmse": _time_to(plain, den2, thresholds)}
             d2.close()
+        for name, path in (more_networks or {}).items():
+            d3 = api.Denoiser(r, seed=0)
+            d3.load(path)
+            log(f"{name} network:")
+            den3 = _denoised_frames(r, cfg, cam, d3, denoise_spps, ref, floor, timer, flops, log)
+            res.setdefault("networks", {})[name] = {"weights": str(path), "denoised": den3,
+                                                    "time_to_relmse": _time_to(plain, den3, thresholds)}
+            d3.close()
 
     # 5. time to each threshold: measured on both arms, raw relMSE (debiased beside it)
     res["time_to_relmse"] = _time_to(plain, den, thresholds)
@@ -307,7 +349,7 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
 
 def train_network(path, views=2000, size=256, full_w=1920, full_h=1080, base_spp=4,
                   extra_spps=(1, 2, 8, 16, 32, 64, 128, 256, 512, 1024), high_spp=256, high_frames=16, iters=10000,
-                  batch=16, crop=128, lr=1e-3, depth=5, seed=0, log=print) -> dict:
+                  batch=16, crop=128, lr=1e-3, depth=5, seed=0, icosphere_views=0, log=print) -> dict:
     """Trains the network shipped with the package and saves it to `path`.
 
     Training set: `views` Cornell variations, each a size x size window of the
@@ -315,21 +357,31 @@ def train_network(path, views=2000, size=256, full_w=1920, full_h=1080, base_spp
     samples and one of extra_spps[v % len] — sharing one target of high_frames x
     high_spp samples from the FP64 accumulation (defaults: 2000 crops of 256x256,
     4-spp inputs, 4096-spp targets; the second input covers the 1..1024-spp frames the
-    time-to-relMSE experiment denoises). Adam over random crop x crop crops."""
+    time-to-relMSE experiment denoises). `icosphere_views` > 0 adds that many windows of
+    seeded icosphere scenes (add_icosphere_views) with the same inputs and targets.
+    Adam over random crop x crop crops."""
     cfg = scenes.cornell_config(spp=high_spp, depth=depth)
+    if icosphere_views:
+        cfg.setGeometryLimit(264)
+        cfg.setGeometryInstanceLimit(264)
     with api.Kuafu(cfg) as r:
         d = api.Denoiser(r, seed=seed)
         t_data = add_training_views(r, cfg, d, views, size, full_w, full_h,
                                     lambda v: [base_spp, extra_spps[v % len(extra_spps)]], high_spp, high_frames,
                                     log=log)
-        log(f"{d.numViews()} training pairs from {views} views in {t_data:.0f} s")
+        if icosphere_views:
+            t_data += add_icosphere_views(r, cfg, d, icosphere_views, size, full_w, full_h,
+                                          lambda v: [base_spp, extra_spps[v % len(extra_spps)]], high_spp,
+                                          high_frames, log=log)
+        log(f"{d.numViews()} training pairs from {views + icosphere_views} views in {t_data:.0f} s")
         t0 = time.perf_counter()
         losses = _train(r, d, iters, batch, crop, lr)
         t_train = time.perf_counter() - t0
         log(f"{iters} Adam steps in {t_train:.0f} s, loss {losses[0]:.4f} -> {losses[-1]:.4f}")
         d.save(path)
         d.close()
-    return {"views": views, "pairs": 2 * views, "size": size, "windows_of": [full_w, full_h],
+    return {"views": views, "icosphere_views": icosphere_views, "pairs": 2 * (views + icosphere_views), "size": size,
+            "windows_of": [full_w, full_h],
             "input_spp": [base_spp] + list(extra_spps), "target_spp": high_spp * high_frames, "iters": iters,
             "batch": batch, "crop": crop, "lr": lr, "loss_curve": losses, "data_seconds": t_data,
             "train_seconds": t_train}
@@ -337,9 +389,11 @@ def train_network(path, views=2000, size=256, full_w=1920, full_h=1080, base_spp
 
 def icosphere_eval(networks: dict, width=1920, height=1080, ref_spp=2048, ref_frame_spp=32,
                    spps=(1, 4, 8, 32, 128), log=print) -> dict:
-    """The networks (name -> parameter file) on content they were not trained on: the
-    256-icosphere scene (glossy, metallic and transmissive spheres, 7 lights, RR, depth 8)
-    at width x height. Reference: two FP64 accumulations of ref_spp / 2 (floor as in run())."""
+    """The networks (name -> parameter file) on the 256-icosphere scene of seed 0 (glossy,
+    metallic and transmissive spheres, 7 lights, RR, depth 8) at width x height: content the
+    Cornell-trained networks never saw; a network trained with add_icosphere_views saw
+    scenes of other seeds. Reference: two FP64 accumulations of ref_spp / 2 (floor as in
+    run())."""
     cfg = scenes.icosphere_config(spp=ref_frame_spp, depth=8)
     cfg.setRussianRoulette(True)
     out = {"scene": f"256 icospheres {width}x{height} depth 8", "reference_spp": ref_spp}
@@ -378,9 +432,11 @@ def main(argv=None):
                     help="train the shipped network (2000 windows of 256x256, 4-spp inputs, 4096-spp targets) "
                          "and save it to PATH instead of running the experiment")
     ap.add_argument("--views", type=int, default=2000, help="training views of --train-network")
+    ap.add_argument("--icosphere-views", type=int, default=0,
+                    help="training views of icosphere scenes added to --train-network's Cornell views")
     a = ap.parse_args(argv)
     if a.train_network:
-        kw = {"views": a.views}
+        kw = {"views": a.views, "icosphere_views": a.icosphere_views}
         if a.train_iters:
             kw["iters"] = a.train_iters
         res = train_network(a.train_network, **kw)

@@ -9,6 +9,8 @@ the same points (straight-through, so its gradients stay FP32): per layer, cosin
 similarity >= 0.985 and relative L2 error <= 0.15 (the CUDA path also rounds every
 activation gradient to BF16; observed per-layer errors are 2-12 %).
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -337,3 +339,59 @@ def test_denoiser_refuses_another_renderers_camera():
         with pytest.raises(N.KfError):
             d.addViewInputs(r2.getScene(), cam2, [1], 4, 1)
         d.close()
+
+
+WEIGHTS = sorted((Path(__file__).resolve().parents[1] / "kuafu_gb300" / "weights").glob("*.kfw"))
+
+
+def _window_errors(r, cfg, cam, d):
+    """relMSE of a 4-spp frame and of its denoised form against a 4096-spp mean."""
+    cfg.setPerPixelSampleRate(256)
+    cfg.setAccumulatingFrames(True)
+    cfg.setSeed(11)
+    r.applyConfig()
+    for _ in range(16):
+        r.run()
+    ref = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32).copy()
+    cfg.setPerPixelSampleRate(4)
+    cfg.setAccumulatingFrames(False)
+    cfg.setSeed(12)
+    r.applyConfig()
+    r.run()
+    noisy = r.downloadAov(cam, N.KF_AOV_RADIANCE_F32).copy()
+    d.apply(cam)
+    den = r.downloadAov(cam, N.KF_AOV_DENOISED_F32).copy()
+    return _relmse(noisy, ref), _relmse(den, ref)
+
+
+@pytest.mark.parametrize("weights", WEIGHTS, ids=[w.stem for w in WEIGHTS])
+def test_packaged_networks_denoise_both_scenes(weights):
+    """Each parameter file under kuafu_gb300/weights loads and, on 256x256 windows of the
+    1920x1080 views (the scale it was trained at), takes a 4-spp frame of a held-out
+    Cornell variation and of the 256-icosphere scene (depth 8, RR) well below the 4-spp
+    input's relMSE."""
+    from kuafu_gb300 import denoise_eval
+    assert len(WEIGHTS) >= 2
+    cases = []
+    cfg = scenes.cornell_config(spp=4, depth=5)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.cornell(r, 256, 256, variation=7)
+        denoise_eval.window_camera(cam, 256, 1920, 1080, 832, 412)
+        d = api.Denoiser(r, seed=0)
+        d.load(str(weights))
+        cases.append(("cornell",) + _window_errors(r, cfg, cam, d))
+        d.close()
+    cfg = scenes.icosphere_config(spp=4, depth=8)
+    cfg.setRussianRoulette(True)
+    with api.Kuafu(cfg) as r:
+        cam = scenes.icospheres(r, 256, 256)
+        denoise_eval.window_camera(cam, 256, 1920, 1080, 832, 412, fov_deg=60.0)
+        d = api.Denoiser(r, seed=0)
+        d.load(str(weights))
+        cases.append(("icospheres",) + _window_errors(r, cfg, cam, d))
+        d.close()
+    assert _tc_error() == 0
+    for name, e_noisy, e_den in cases:
+        print(f"{weights.stem} {name}: relMSE 4 spp {e_noisy:.4e}, denoised {e_den:.4e}")
+        assert np.isfinite(e_den)
+        assert e_den < 0.25 * e_noisy, (name, e_noisy, e_den)
