@@ -169,10 +169,19 @@ struct Geometry {
                                              (uint32_t)vertices.size(), indices.data(), (uint32_t)indices.size(),
                                              matIndex.data(), (uint32_t)matIndex.size(), &g));
             detail::check(kf_geometry_set_flags(g, isOpaque, hideRender, dynamic));
+            pushed_ = flags();
             handle_.reset(g, [](kf_geometry p) { kf_geometry_release(p); });
             initialized = true;
         }
         return handle_.get();
+    }
+    // isOpaque / hideRender / dynamic edited after submission reach the next frame, as in
+    // kuafu, which reads them when it rebuilds the TLAS every frame (rt.cpp:156)
+    void pushFlags() {
+        if (handle_ && flags() != pushed_) {
+            detail::check(kf_geometry_set_flags(handle_.get(), isOpaque, hideRender, dynamic));
+            pushed_ = flags();
+        }
     }
     void adopt(kf_geometry g) {
         handle_.reset(g, [](kf_geometry p) { kf_geometry_release(p); });
@@ -187,7 +196,9 @@ struct Geometry {
     }
 
   private:
+    int flags() const { return (isOpaque ? 1 : 0) | (hideRender ? 2 : 0) | (dynamic ? 4 : 0); }
     std::shared_ptr<struct kf_geometry_s> handle_;
+    int pushed_ = -1;
 };
 
 // include/core/geometry.hpp:48-54
@@ -501,6 +512,9 @@ class Scene {
             }
     }
 
+    void pushGeometryFlags() {
+        for (auto& g : geometries_) g->pushFlags();
+    }
     // kuafu re-reads the light objects every frame (uploadLightBuffers); so does the facade.
     void pushLights() {
         if (dlight_) {
@@ -568,6 +582,7 @@ class Kuafu {
     Kuafu& operator=(const Kuafu&) = delete;
 
     void run() {
+        current_->pushGeometryFlags();
         current_->pushLights();
         detail::check(kf_renderer_run(r_));
     }

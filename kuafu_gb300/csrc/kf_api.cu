@@ -622,7 +622,7 @@ KF_API int kf_geometry_recalculate_normals(kf_geometry g) {
     return guarded([&] {
         REQ(g, "null geometry");
         recalculate_normals(g->vertices, g->indices);
-        ++g->version;
+        ++g->vert_version;
     });
 }
 KF_API int kf_geometry_get_info(kf_geometry g, uint32_t* nv, uint32_t* ni) {

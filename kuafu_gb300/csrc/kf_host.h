@@ -26,7 +26,8 @@ struct kf_geometry_s {
     bool opaque = true;
     bool hide_render = false;
     bool dynamic_ = false;
-    uint64_t version = 1;
+    uint64_t version = 1;       // material and flags (opaque, hideRender): instance records and TLAS
+    uint64_t vert_version = 1;  // vertex data (recalculated normals): geometry upload and BLAS
 };
 
 struct kf_instance_s {
@@ -93,6 +94,8 @@ struct SceneGpu {
     uint32_t built_bvh_key = 0;  // builder, leaf size and sharing the BLAS were built with
     uint64_t built_inst_stamp = 0;
     uint64_t built_xform_stamp = 0;
+    uint64_t built_vert_sum = 0;   // sum of the geometries' vert_version the buffers were built from
+    uint64_t built_flag_sum = 0;   // sum of the geometries' version the instance records hold
     std::vector<kf::Node4> tlas_host_nodes; // TLAS topology kept for refits
     std::vector<uint32_t> tlas_host_inst;
     uint64_t tlas_refits = 0;

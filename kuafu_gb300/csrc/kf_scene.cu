@@ -230,17 +230,41 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
     cudaStream_t st = r->stream;
     SceneGpu& G = s->gpu;
     bool rebuilt_geom = false;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    const bool timing = true;
-    if (timing) {
-        KF_CUDA_CHECK(cudaEventCreate(&e0));
-        KF_CUDA_CHECK(cudaEventCreate(&e1));
-        KF_CUDA_CHECK(cudaEventRecord(e0, st));
-    }
-    bool built_any = false, refitted = false;
+    // build timing (bvh_build_ms): events around the update, waited on only when something
+    // was built, so that a frame without changes queues behind the previous one unblocked
+    struct SyncEvents {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~SyncEvents() {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } ev;
+    KF_CUDA_CHECK(cudaEventCreate(&ev.e0));
+    KF_CUDA_CHECK(cudaEventCreate(&ev.e1));
+    KF_CUDA_CHECK(cudaEventRecord(ev.e0, st));
+    bool built_any = false, refitted = false, matidx_changed = false;
     const uint32_t bvh_key = 1u | (r->cfg.bvh_builder << 1) | (r->cfg.blas_leaf_size << 2) |
                              ((r->cfg.blas_share ? 1u : 0u) << 8);
-    if (G.built_geom_stamp != s->geom_stamp || G.built_bvh_key != bvh_key) {
+    // a geometry's versions only grow, so their sums change whenever one of them does
+    uint64_t vert_sum = 0, flag_sum = 0;
+    for (const kf_geometry_s* g : s->geometries) {
+        vert_sum += g->vert_version;
+        flag_sum += g->version;
+    }
+    const bool geom_changed =
+        G.built_geom_stamp != s->geom_stamp || G.built_bvh_key != bvh_key || G.built_vert_sum != vert_sum;
+    if (geom_changed || G.built_material_version != g_material_version) {
+        // every triangle must name an existing material (the kernels index the table
+        // unchecked); checked before anything is uploaded or marked as built, so that a
+        // refused scene leaves no stale index on the device
+        for (const kf_geometry_s* g : s->geometries) {
+            const size_t ntri = g->indices.size() / 3;
+            for (size_t t = 0; t < ntri; ++t)
+                KF_REQUIRE(g->mat_index[t] < g_materials.size(), KF_ERR_OUT_OF_RANGE,
+                           "a geometry's matIndex names a material that does not exist");
+        }
+    }
+    if (geom_changed) {
         built_any = true;
         rebuilt_geom = true;
         const size_t ng = s->geometries.size();
@@ -439,15 +463,20 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         G.blas_node_count = node_base;
         G.built_geom_stamp = s->geom_stamp;
         G.built_bvh_key = bvh_key;
+        G.built_vert_sum = vert_sum;
     }
     if (G.built_material_version != g_material_version || rebuilt_geom) {
         std::vector<kf_material_gpu> mats = flatten_materials();
-        // every triangle must name an existing material: the kernels index the table unchecked
-        for (const kf_geometry_s* g : s->geometries) {
-            const size_t ntri = g->indices.size() / 3;
-            for (size_t t = 0; t < ntri; ++t)
-                KF_REQUIRE(g->mat_index[t] < mats.size(), KF_ERR_OUT_OF_RANGE,
-                           "a geometry's matIndex names a material that does not exist");
+        if (!rebuilt_geom) {
+            // the per-triangle material indices follow the geometries' current ones
+            // (Geometry::setMaterial after the first upload, or a cleared and refilled table)
+            std::vector<uint32_t> mat;
+            mat.reserve(G.matidx.count);
+            for (const kf_geometry_s* g : s->geometries)
+                mat.insert(mat.end(), g->mat_index.begin(), g->mat_index.begin() + g->indices.size() / 3);
+            KF_REQUIRE(mat.size() == G.matidx.count, KF_ERR_INTERNAL, "material index count changed");
+            G.matidx.upload(mat.data(), mat.size(), st);
+            matidx_changed = true;
         }
         if (mats.empty()) mats.push_back(kf_material_gpu{});
         G.materials.upload(mats.data(), mats.size(), st);
@@ -540,7 +569,9 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
             ids.push_back((uint32_t)i);
         }
     };
-    const bool set_changed = rebuilt_geom || G.built_inst_stamp != s->inst_stamp;
+    // the instance records carry each geometry's opaque and hidden flags (kuafu reads
+    // hideRender when it rebuilds the TLAS every frame, rt.cpp:156): a change rebuilds
+    const bool set_changed = rebuilt_geom || G.built_inst_stamp != s->inst_stamp || G.built_flag_sum != flag_sum;
     if (!set_changed && G.built_xform_stamp != s->xform_stamp) {
         // Transforms moved, the instance set did not (RayTracer::updateTlas every frame,
         // context.cpp:334-341): new world->object rows and world boxes; the TLAS keeps its
@@ -659,17 +690,16 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         }
         G.built_inst_stamp = s->inst_stamp;
         G.built_xform_stamp = s->xform_stamp;
+        G.built_flag_sum = flag_sum;
     }
     if (built_any || rebuilt_geom) ++G.generation;            // buffers may have moved: recapture graphs
-    if (built_any || rebuilt_geom || refitted) ++G.content_version; // contents changed: recopy batch pools
-    if (timing) {
-        KF_CUDA_CHECK(cudaEventRecord(e1, st));
-        KF_CUDA_CHECK(cudaEventSynchronize(e1));
+    if (built_any || rebuilt_geom || refitted || matidx_changed) ++G.content_version; // contents changed: recopy batch pools
+    if (built_any) {
+        KF_CUDA_CHECK(cudaEventRecord(ev.e1, st));
+        KF_CUDA_CHECK(cudaEventSynchronize(ev.e1));
         float ms = 0.0f;
-        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
-        if (built_any) r->stats.bvh_build_ms += ms;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        KF_CUDA_CHECK(cudaEventElapsedTime(&ms, ev.e0, ev.e1));
+        r->stats.bvh_build_ms += ms;
     }
     // lights: every frame, like uploadUniformBuffers
     kf_dir_light_ubo d;

@@ -1172,8 +1172,26 @@ void inverse4(const double* m, double* inv) {
 // ---------------------------------------------------------------------------
 extern "C" {
 
+// The references a flat scene holds stay inside its arrays: vertex indices, material
+// indices and instance geometry indices (the product refuses such a scene before its
+// upload with KF_ERR_OUT_OF_RANGE; here it is return code 3).
+static bool scene_consistent(const kf_flat_scene* s) {
+    for (uint32_t i = 0; i < s->num_instances; ++i)
+        if (s->instances[i].geometry_index >= s->num_geometries) return false;
+    for (uint32_t gi = 0; gi < s->num_geometries; ++gi) {
+        const kf_flat_geometry& g = s->geometries[gi];
+        for (uint32_t t = 0; t < g.num_triangles; ++t) {
+            if (g.mat_index[t] >= s->num_materials) return false;
+            for (int k = 0; k < 3; ++k)
+                if (g.indices[3 * t + k] >= g.num_vertices) return false;
+        }
+    }
+    return true;
+}
+
 int kf_oracle_render(const kf_flat_scene* scene, const kf_oracle_view* view, kf_oracle_out* out) {
     if (!scene || !view || !out || !view->camera || view->width == 0 || view->height == 0) return 1;
+    if (!scene_consistent(scene)) return 3;
     const uint32_t cw = view->crop_w ? view->crop_w : view->width;
     const uint32_t ch = view->crop_h ? view->crop_h : view->height;
     if (view->x0 + cw > view->width || view->y0 + ch > view->height) return 2;
@@ -1214,6 +1232,7 @@ int kf_oracle_render(const kf_flat_scene* scene, const kf_oracle_view* view, kf_
 
 int kf_oracle_trace(const kf_flat_scene* scene, const float* rays, uint32_t n, uint32_t use_bvh, kf_hit* out) {
     if (!scene || (!rays && n) || (!out && n)) return 1;
+    if (!scene_consistent(scene)) return 3;
     SceneAccel sa;
     prepare_accel(sa, scene, use_bvh != 0);
     for (uint32_t i = 0; i < n; ++i) {

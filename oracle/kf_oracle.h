@@ -52,7 +52,8 @@ typedef struct kf_oracle_out {
     uint64_t rays_shadow;
 } kf_oracle_out;
 
-/* Render one frame's samples for a crop (PathTrace.rgen main). Returns 0 on success. */
+/* Render one frame's samples for a crop (PathTrace.rgen main). Returns 0 on success, 3 when
+ * a vertex, material or geometry index of the scene is out of range. */
 int kf_oracle_render(const kf_flat_scene* scene, const kf_oracle_view* view, kf_oracle_out* out);
 
 /* Closest hit of arbitrary world-space rays against the scene (traceRayEXT, rgen:97-107).

@@ -314,3 +314,78 @@ def test_builders_with_coincident_triangles(builder):
     p = hits["prim"][hit]
     assert (p == 200).any() and (p == 0).any()
     assert not ((p > 0) & (p < 200)).any() and not ((p > 200) & (p < 300)).any()
+
+
+@pytest.mark.parametrize("builder", [0, 1, 2])
+@pytest.mark.parametrize("instances", [1, 5])
+def test_builders_on_tiny_geometries(builder, instances):
+    """BLAS of 1, 2, 3 and 5 triangles (a one-leaf BLAS, and trees of one or two levels),
+    a second geometry with the 3-triangle one's positions and indices (a shared BLAS), and a
+    TLAS of one instance or of five: every builder gives the oracle's brute-force hits."""
+    rng = np.random.default_rng(11)
+
+    def geometry(n):
+        # n roughly equilateral triangles of circumradius 0.3 facing the camera (-x), their
+        # centres spread over [-0.3, 0.3] in y and z, depth jittered by 0.05
+        pos = []
+        for _ in range(n):
+            c = np.array([rng.uniform(-0.05, 0.05), rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3)])
+            a0 = rng.uniform(0.0, 2.0 * np.pi)
+            for k in range(3):
+                a = a0 + 2.0 * np.pi * k / 3.0
+                pos.append(c + (rng.uniform(-0.05, 0.05), 0.3 * np.cos(a), 0.3 * np.sin(a)))
+        return np.array(pos), np.arange(3 * n)
+
+    shapes = [geometry(n) for n in (1, 2, 3, 5)]
+    shapes.append(shapes[2])
+    spp, depth, w, h = 1, 1, 48, 40
+    cfg = scenes.cornell_config(spp=spp, depth=depth)
+    cfg.setDebugOutputs(True)
+    cfg.setBvhBuilder(builder)
+    with api.Kuafu(cfg) as r:
+        s = r.getScene()
+        for k, (pos, idx) in enumerate(shapes[:instances]):
+            g = api.Geometry.from_arrays(pos, idx)
+            g.setMaterial(api.NiceMaterial(diffuseColor=(0.7, 0.7, 0.7)))
+            s.submitGeometry(g)
+            m = np.eye(4)
+            m[:3, :3] *= 2.5 if instances == 1 else 1.0
+            m[:3, 3] = (0.2 * k, -0.9 + 0.45 * k, 0.3 * (k % 2) - 0.15) if instances > 1 else (0.0, 0.0, 0.0)
+            s.submitGeometryInstance(api.instance(g, m))
+        cam = s.createCamera(w, h)
+        s.setCamera(cam)
+        cam.setPosition((-2.0, 0.0, 0.0))
+        cam.setFront((1.0, 0.0, 0.0))
+        cam.setUp((0.0, 0.0, 1.0))
+        scenes.pinhole(cam, w, h, 60.0)
+        r.run()
+        hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, spp)
+        ref = O.render(s.export(), cam.ubo(), w, h, O.push_constants(spp, depth), seed=0, frame=0, camera_index=1)
+    rh = ref["hits"]
+    assert np.array_equal(hits["instance"], rh["instance"])
+    hit = rh["instance"] != 0xFFFFFFFF
+    assert hit.mean() > 0.05
+    assert len(np.unique(rh["instance"][hit])) == instances
+    assert np.array_equal(hits["prim"][hit], rh["prim"][hit])
+    assert np.array_equal(hits["t"][hit], rh["t"][hit])
+    assert np.array_equal(hits["u"][hit], rh["u"][hit]) and np.array_equal(hits["v"][hit], rh["v"][hit])
+
+
+def test_out_of_range_material_index_is_refused():
+    """A geometry whose matIndex names a material that does not exist is refused on the
+    host, before any upload or launch, and the renderer stays usable."""
+    cfg = scenes.cornell_config(spp=1, depth=1)
+    with api.Kuafu(cfg) as r:
+        s = r.getScene()
+        g = api.Geometry.from_arrays([(1.0, -0.5, -0.5), (1.0, 0.5, -0.5), (1.0, 0.0, 0.5)], [0, 1, 2],
+                                     mat_index=[1 << 30])
+        s.submitGeometry(g)
+        s.submitGeometryInstance(api.instance(g, np.eye(4)))
+        cam = s.createCamera(16, 16)
+        s.setCamera(cam)
+        with pytest.raises(N.KfError, match="material"):
+            r.run()
+        g.setMaterial(api.NiceMaterial(diffuseColor=(0.5, 0.5, 0.5)))
+        r.run()
+        r.synchronize()
+        assert r.downloadLatestFrame(cam).shape == (16, 16, 4)

@@ -136,3 +136,43 @@ def test_light_swap_under_graph_replay_matches_direct_launch():
             assert not np.array_equal(first, paths)
             outs.append(paths)
     assert np.array_equal(outs[0], outs[1])
+
+
+def _matches_oracle(r, s, cam, frame):
+    paths = r.downloadAov(cam, N.KF_AOV_PATH_RADIANCE, SPP).copy()
+    hits = r.downloadAov(cam, N.KF_AOV_PRIMARY_HITS, SPP).copy()
+    ref = O.render(s.export(), cam.ubo(), 64, 48, O.push_constants(SPP, DEPTH, clear=(0.1, 0.1, 0.1, 1.0)),
+                   seed=0, frame=frame, camera_index=1, use_bvh=True)
+    assert np.array_equal(hits["instance"], ref["hits"]["instance"])
+    hit = ref["hits"]["instance"] != 0xFFFFFFFF
+    assert np.array_equal(hits["prim"][hit], ref["hits"]["prim"][hit])
+    g = paths[..., :3].astype(np.float64)
+    c = ref["paths"].astype(np.float64)
+    assert ((np.abs(g - c) / np.maximum(np.abs(c), 1e-6)).max(axis=-1) <= 1e-4).mean() >= 0.999
+    return paths, hits
+
+
+def test_material_and_visibility_changes_between_frames():
+    """Geometry::setMaterial, hideRender and isOpaque changed between frames reach the next
+    frame (kuafu reads a geometry's hideRender and opacity when it rebuilds the TLAS every
+    frame, rt.cpp:156, context.cpp:328-341): each frame equals the oracle's render of the
+    scene as it then is, under graph replay."""
+    with api.Kuafu(_cfg()) as r:
+        s, cam, insts = _scene(r, _transforms(16, 5))
+        red, blue = insts[0].geometry, insts[1].geometry
+        r.run()
+        first, hits0 = _matches_oracle(r, s, cam, 0)
+        blue_ids = {i for i in range(1, 16, 2)}
+        assert np.isin(hits0["instance"], list(blue_ids)).any()
+        red.setMaterial(api.NiceMaterial(diffuseColor=(0.1, 0.9, 0.1), metallic=1.0, roughness=0.3))
+        r.run()
+        second, _ = _matches_oracle(r, s, cam, 1)
+        assert not np.array_equal(first, second)
+        blue.setFlags(opaque=True, hide_render=True)
+        r.run()
+        _, hits2 = _matches_oracle(r, s, cam, 2)
+        assert not np.isin(hits2["instance"], list(blue_ids)).any()
+        blue.setFlags(opaque=True, hide_render=False)
+        r.run()
+        _, hits3 = _matches_oracle(r, s, cam, 3)
+        assert np.isin(hits3["instance"], list(blue_ids)).any()

@@ -43,3 +43,61 @@ def test_oracle_flattened_icosphere_scene_equals_the_product_export():
         assert bytes(a.plights) == bytes(b.plights)
         assert bytes(a.alights) == bytes(b.alights)
         assert bytes(cam.ubo()) == bytes(fs.camera)
+
+
+def test_oracle_refuses_out_of_range_references():
+    """A flat scene whose material, vertex or geometry index points past its arrays is
+    refused by both oracle entry points (return code 3) instead of being read out of bounds;
+    the product refuses such a scene before its upload. The mistakes are planted in copies
+    of the exported scene's records."""
+    import pytest
+
+    from kuafu_gb300 import _native as N
+    from oracle import oracle as O
+
+    cfg = scenes.cornell_config(spp=1, depth=1)
+    cfg.setHostOnly(True)
+    with api.Kuafu(cfg) as r:
+        s = r.getScene()
+        g = api.Geometry.from_arrays([(1.0, -0.5, -0.5), (1.0, 0.5, -0.5), (1.0, 0.0, 0.5)], [0, 1, 2])
+        g.setMaterial(api.NiceMaterial(diffuseColor=(0.5, 0.5, 0.5)))
+        s.submitGeometry(g)
+        s.submitGeometryInstance(api.instance(g, np.eye(4)))
+        cam = s.createCamera(8, 8)
+        s.setCamera(cam)
+        cam.setPosition((-2.0, 0.0, 0.0))
+        cam.setFront((1.0, 0.0, 0.0))
+        cam.setUp((0.0, 0.0, 1.0))
+        flat = s.export()
+        ubo = cam.ubo()
+        rays = np.array([[-2.0, 0.0, 0.0, 1e-3, 1.0, 0.0, 0.0, 1e6]], np.float32)
+        assert O.trace(flat, rays)["instance"][0] == 0
+        O.render(flat, ubo, 8, 8, O.push_constants(1, 1))
+
+        def planted(field, value, where="geometry"):
+            f2 = N.kf_flat_scene.from_buffer_copy(flat)
+            keep = []
+            if where == "geometry":
+                g2 = N.kf_flat_geometry.from_buffer_copy(flat.geometries[0])
+                n = 3 * g2.num_triangles if field == "indices" else g2.num_triangles
+                arr = np.ctypeslib.as_array(getattr(g2, field), (n,)).copy()
+                arr[0] = value(g2)
+                setattr(g2, field, arr.ctypes.data_as(type(getattr(g2, field))))
+                geoms = (N.kf_flat_geometry * 1)(g2)
+                f2.geometries = C.cast(geoms, C.POINTER(N.kf_flat_geometry))
+                keep += [arr, geoms]
+            else:
+                i2 = N.kf_flat_instance.from_buffer_copy(flat.instances[0])
+                i2.geometry_index = flat.num_geometries
+                insts = (N.kf_flat_instance * 1)(i2)
+                f2.instances = C.cast(insts, C.POINTER(N.kf_flat_instance))
+                keep.append(insts)
+            return f2, keep
+
+        for f2, keep in (planted("mat_index", lambda g2: flat.num_materials),
+                         planted("indices", lambda g2: g2.num_vertices),
+                         planted(None, None, where="instance")):
+            with pytest.raises(RuntimeError, match="failed: 3"):
+                O.render(f2, ubo, 8, 8, O.push_constants(1, 1))
+            with pytest.raises(RuntimeError):
+                O.trace(f2, rays)
