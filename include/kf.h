@@ -331,10 +331,13 @@ KF_API int kf_renderer_measure_l2_read(kf_renderer r, uint64_t bytes, uint32_t p
 /* ---- tensor-core building blocks of the learned denoiser (device pointers; no
  * counterpart in kuafu, whose OptiX denoiser is closed code, denoiser.cpp:257-316) ---- */
 /* y[n,y,x,y_coff+co] = act(bias[co] + sum x[n,y+dy,x+dx,ci] * w[tap][co][ci]), NHWC BF16,
- * zero padding, FP32 accumulation; w: [9][w_rows][cin], w_rows % 16 == 0, cin % 32 == 0. */
+ * zero padding, FP32 accumulation; w: [9][w_rows][cin], w_rows % 16 == 0, cin a multiple of
+ * 32 (or 16 for images at least 96 wide); x, weight and y 16-byte aligned. */
 KF_API int kf_conv3x3_bf16(const void* x, int n, int h, int w, int cin, const void* weight, int w_rows,
                            const float* bias, int cout, int relu, void* y, int y_cstride, int y_coff, void* stream);
-/* d[m][n] += sum_k a[m][k] * b[n][k], BF16 K-major operands, FP32 accumulation (split-K atomics). */
+/* d[m][n] += sum_k a[m][k] * b[n][k], BF16 K-major operands (16-byte aligned, k % 8 == 0),
+ * FP32 accumulation into d (row stride ldd >= n) by split-K atomics: d is added to, not
+ * overwritten. */
 KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, float* d, int ldd, int splits,
                            void* stream);
 /* Error word of the tensor-core kernels (0 = none; set when a bounded wait expired); cleared on read. */
@@ -385,7 +388,8 @@ KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d);
  * 6..8 normal, 9 t / (1 + t), 10 log2(samples) / 8, rest 0); base [n][h][w] float4 FP32
  * residual added to the network output (NULL = none; the renderer passes g(noisy));
  * out [n][h][w][4] FP32 prediction in g space (channel 3 = 0); target [n][h][w] float4
- * linear radiance; h, w % 16 == 0. train_step computes the L1 + gradient loss in g space
+ * linear radiance; h, w % 16 == 0; base, target and the buffers kf_denoiser_camera_features
+ * fills 16-byte aligned. train_step computes the L1 + gradient loss in g space
  * and its gradients (copied to grads_dev, may be NULL, FP32, num_params) and, if apply,
  * one Adam step with learning rate lr. */
 KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* base, int n, int h, int w, float* out);
@@ -400,8 +404,8 @@ KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* 
                                   int h, int w, float lr, float* grads_dev, int apply, float* loss);
 
 /* ---- FP64 relative-MSE reduction: mean over pixels and channels of
- * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels, reduced in FP64;
- * num_pixels > 0 ---- */
+ * (x - ref)^2 / (ref^2 + eps), rgb of float4 pixels (16-byte aligned images), reduced in
+ * FP64; num_pixels > 0 ---- */
 KF_API int kf_relmse(kf_renderer r, const float* x_dev, const float* ref_dev, uint64_t num_pixels, double eps,
                      double* out);
 

@@ -1245,6 +1245,7 @@ KF_API int kf_relmse(kf_renderer r, const float* x, const float* ref, uint64_t n
     return guarded([&] {
         REQ(r && x && ref && out, "null argument");
         REQ(n > 0, "relMSE over zero pixels");
+        REQ(((uintptr_t)x & 15) == 0 && ((uintptr_t)ref & 15) == 0, "images must be 16-byte aligned (float4 pixels)");
         require_device(r);
         const uint32_t blocks = (uint32_t)std::max(1, std::min(r->num_sms * 4, (int)((n + 255) / 256)));
         if (r->scratch64.count < (size_t)blocks + 1) r->scratch64.resize(blocks + 1, r->stream);
@@ -1424,9 +1425,13 @@ KF_API int kf_renderer_set_denoiser(kf_renderer r, kf_denoiser d) {
         r->denoiser = d;
     });
 }
+// float4 and 16-byte BF16 accesses: base, target and feature buffers are 16-byte aligned
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 KF_API int kf_denoiser_forward(kf_denoiser d, const void* feat, const float* base, int n, int h, int w, float* out) {
     return guarded([&] {
         REQ(feat && out && n > 0 && h > 0 && w > 0, "invalid tensor");
+        REQ(aligned16(base), "base must be 16-byte aligned");
         check_denoiser(d);
         denoiser_forward(d, feat, base, n, h, w, out);
         sync_stream(denoiser_renderer(d));
@@ -1444,6 +1449,7 @@ KF_API int kf_denoiser_camera_features(kf_denoiser d, kf_camera c, void* feat_de
         *wp = (cam->target_w + 15) / 16 * 16;
         if (!feat_dev && !base_dev) return;
         REQ(feat_dev && base_dev, "both feature and base buffers are needed");
+        REQ(aligned16(feat_dev) && aligned16(base_dev), "feature and base buffers must be 16-byte aligned");
         kf_renderer_s* r = denoiser_renderer(d);
         KF_CUDA_CHECK(cudaSetDevice(r->device));
         denoiser_camera_features(d, cam, feat_dev, base_dev);
@@ -1454,6 +1460,7 @@ KF_API int kf_denoiser_train_step(kf_denoiser d, const void* feat, const float* 
                                   int h, int w, float lr, float* grads_dev, int apply, float* loss) {
     return guarded([&] {
         REQ(feat && target && n > 0 && h > 0 && w > 0, "invalid tensor");
+        REQ(aligned16(base) && aligned16(target), "base and target must be 16-byte aligned");
         check_denoiser(d);
         const float l = denoiser_train_step(d, feat, base, target, n, h, w, lr, grads_dev, apply != 0);
         if (loss) *loss = l;

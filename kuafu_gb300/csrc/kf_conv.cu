@@ -845,8 +845,12 @@ bool conv3x3_bf16(const __nv_bfloat16* x, int N, int H, int W, int Cin, const __
     KF_REQUIRE(Cout > 0 && Cout <= Cout_rows && Cout_rows % 16 == 0, KF_ERR_INVALID_ARGUMENT,
                "conv3x3: weight rows must be a multiple of 16 covering the output channels");
     KF_REQUIRE(y_coff >= 0 && y_coff + Cout <= y_cstride, KF_ERR_INVALID_ARGUMENT, "conv3x3: output slice");
-    KF_REQUIRE(((uintptr_t)x & 15) == 0 && ((uintptr_t)w & 15) == 0, KF_ERR_INVALID_ARGUMENT,
-               "conv3x3: tensors must be 16-byte aligned");
+    // the epilogue stores 8 BF16 channels as one 16-byte word where the slice allows it
+    KF_REQUIRE(((uintptr_t)x & 15) == 0 && ((uintptr_t)w & 15) == 0 && ((uintptr_t)y & 15) == 0 &&
+                   ((uintptr_t)y_f32 & 3) == 0,
+               KF_ERR_INVALID_ARGUMENT, "conv3x3: tensors must be 16-byte aligned (FP32 output: 4-byte)");
+    KF_REQUIRE(!fuse || !fuse->pool_out || (((uintptr_t)fuse->pool_out & 15) == 0 && Cout % 8 == 0),
+               KF_ERR_INVALID_ARGUMENT, "conv3x3: pooled output must be 16-byte aligned with Cout % 8 == 0");
     const int halo = conv3x3_halo(x, N, H, W, Cin, w, Cout_rows, bias, Cout, relu, y, y_cstride, y_coff, st, y_f32,
                                   fuse);
     if (halo) return halo == 2;
@@ -897,6 +901,8 @@ void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, 
     KF_REQUIRE(K % 8 == 0, KF_ERR_INVALID_ARGUMENT, "gemm: K must be a multiple of 8 (16-byte rows)");
     KF_REQUIRE(((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0, KF_ERR_INVALID_ARGUMENT,
                "gemm: operands must be 16-byte aligned");
+    KF_REQUIRE(d && ((uintptr_t)d & 3) == 0 && ldd >= N, KF_ERR_INVALID_ARGUMENT,
+               "gemm: output must be 4-byte aligned with ldd >= n");
     const int n_tile = N <= 256 ? ((N + 15) / 16) * 16 : 128;
     const uint64_t adims[2] = {(uint64_t)K, (uint64_t)M};
     const uint64_t astr[1] = {(uint64_t)K * 2};

@@ -1644,6 +1644,10 @@ extern "C" KF_API int kf_relmse_noalloc(const float* x_dev, const float* ref_dev
         kf::set_last_error("kf_relmse_noalloc: null pointer or zero pixels");
         return KF_ERR_INVALID_ARGUMENT;
     }
+    if (((uintptr_t)x_dev & 15) != 0 || ((uintptr_t)ref_dev & 15) != 0) { // float4 pixel loads
+        kf::set_last_error("kf_relmse_noalloc: images must be 16-byte aligned");
+        return KF_ERR_INVALID_ARGUMENT;
+    }
     if (num_pixels > kNoAllocMaxPixels) {
         kf::set_last_error("kf_relmse_noalloc: more than 268435456 pixels per call exceed the limit of its static "
                            "scratch; use kf_relmse");

@@ -220,3 +220,30 @@ def test_relmse_entry_points_reject_zero_pixels():
     assert lib.kf_relmse(r._h, C.c_void_p(16), C.c_void_p(16), 0, 1e-2, C.byref(got)) == 1
     assert b"zero pixels" in lib.kf_last_error()
     r.close()
+
+
+def test_tensor_kernel_arguments_are_checked_before_any_launch():
+    """kf_conv3x3_bf16, kf_gemm_bf16_tn and kf_relmse_noalloc refuse shapes and alignments
+    their TMA loads and vector loads and stores cannot take, before touching the device (KF_ERR_INVALID_ARGUMENT); the
+    pointer values below are never dereferenced."""
+    lib = N.load()
+    INVALID = 1  # KF_ERR_INVALID_ARGUMENT
+    A = 1 << 20  # a 16-byte aligned stand-in address
+
+    def conv(x=A, cin=32, w=A, rows=32, cout=32, y=A, cs=32, co=0, n=1, h=8, wd=8):
+        return lib.kf_conv3x3_bf16(x, n, h, wd, cin, w, rows, None, cout, 1, y, cs, co, None)
+
+    assert conv(y=A + 2) == INVALID          # output not 16-byte aligned
+    assert conv(x=A + 8) == INVALID          # input not 16-byte aligned
+    assert conv(cin=48) == INVALID           # channels neither 16 nor a multiple of 32
+    assert conv(rows=24, cout=24) == INVALID  # weight rows not a multiple of 16
+    assert conv(co=8, cs=32) == INVALID      # output slice past the channel stride
+    assert conv(n=0) == INVALID
+    assert conv(y=0) == INVALID
+    assert lib.kf_gemm_bf16_tn(A, 128, A, 64, 64, A + 2, 64, 1, None) == INVALID   # output misaligned
+    assert lib.kf_gemm_bf16_tn(A, 128, A, 64, 64, A, 32, 1, None) == INVALID       # ldd < n
+    assert lib.kf_gemm_bf16_tn(A, 128, A, 64, 60, A, 64, 1, None) == INVALID       # k % 8 != 0
+    assert lib.kf_gemm_bf16_tn(A + 8, 128, A, 64, 64, A, 64, 1, None) == INVALID   # operand misaligned
+    got = C.c_double()
+    assert lib.kf_relmse_noalloc(C.c_void_p(A + 4), C.c_void_p(A), 16, 1e-2, None, C.byref(got)) == INVALID
+    assert b"16-byte aligned" in lib.kf_last_error()
