@@ -297,6 +297,10 @@ def time_to_relmse_summary() -> dict:
                                         for d in res["networks"]["mixed"]["denoised"]]}
                           if "mixed" in res.get("networks", {}) else None),
         "icosphere_scene": ico,
+        # relMSE 1e-3 on the icosphere scene, per network: plain accumulation against one frame
+        # plus one inference, both measured against the same 8192-spp reference
+        "icosphere_headline": {n: next(r for r in ico[n + "_time_to_relmse"] if r["tau"] == 1e-3)["relmse"]
+                               for n in nets if n + "_time_to_relmse" in ico},
         "denoiser_roofline": {"bound": "tensor", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s",
                               "frac": (ach / peak_tf) if peak_tf else None,
                               "flops_per_frame": res["denoiser_flops_per_frame"],

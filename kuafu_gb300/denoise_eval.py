@@ -223,6 +223,37 @@ def _denoised_frames(r, cfg, cam, d, spps, ref, floor, timer, flops, log, seed=9
     return den
 
 
+def _plain_curve(r, cfg, cam, ref, floor, timer, frame_spp, checkpoint_step, max_spp, tau_min, seed=7):
+    """Plain accumulation of frame_spp-sample frames into the FP64 sum (seed `seed`): the
+    cumulative CUDA-event time of the frames and the relMSE of the running mean against
+    ref at powers of two up to 1024 spp, then every checkpoint_step spp, until the relMSE
+    is at most tau_min or max_spp is reached (the evaluations are not timed). Returns
+    (checkpoints, samples accumulated)."""
+    cfg.setSeed(seed)
+    cfg.setPerPixelSampleRate(frame_spp)
+    cfg.setAccumulatingFrames(True)
+    cfg.setUseDenoiser(False)
+    r.applyConfig()
+    r.run()  # graph capture outside the timed frames; the reset below discards this frame
+    r.synchronize()
+    r.resetFrame()
+    plain = []
+    t_ms, spp = 0.0, 0
+    next_cp = frame_spp
+    while spp < max_spp:
+        with timer:
+            r.run()
+        t_ms += timer.ms
+        spp += frame_spp
+        if spp >= next_cp:
+            e = _gpu_relmse(r, _fp64_mean(r, cam), ref)
+            plain.append({"spp": spp, "ms": t_ms, "relmse": e, "relmse_debiased": e - floor})
+            next_cp = next_cp * 2 if next_cp < 1024 else next_cp + checkpoint_step
+            if e <= tau_min:
+                break
+    return plain, spp
+
+
 def _time_to(plain, den, thresholds):
     """For each threshold: measured plain time, denoised time, ratio (raw and debiased relMSE)."""
     ttr = []
@@ -264,28 +295,8 @@ def run(width=1920, height=1080, ref_spp=40960, ref_frame_spp=256, plain_frame_s
         # 2. plain accumulation (FP64 sum of equal frames), measured until the smallest
         #    threshold is reached
         timer = _Timer(r)
-        tau_min = min(thresholds)
-        cfg.setSeed(7)
-        cfg.setPerPixelSampleRate(plain_frame_spp)
-        cfg.setAccumulatingFrames(True)
-        r.applyConfig()
-        r.run()  # graph capture outside the timed frames; the reset below discards this frame
-        r.synchronize()
-        r.resetFrame()
-        plain = []
-        t_ms, spp = 0.0, 0
-        next_cp = plain_frame_spp
-        while spp < plain_max_spp:
-            with timer:
-                r.run()
-            t_ms += timer.ms
-            spp += plain_frame_spp
-            if spp >= next_cp:
-                e = _gpu_relmse(r, _fp64_mean(r, cam), ref)
-                plain.append({"spp": spp, "ms": t_ms, "relmse": e, "relmse_debiased": e - floor})
-                next_cp = next_cp * 2 if next_cp < 1024 else next_cp + plain_checkpoint_step
-                if e <= tau_min:
-                    break
+        plain, spp = _plain_curve(r, cfg, cam, ref, floor, timer, plain_frame_spp, plain_checkpoint_step,
+                                  plain_max_spp, min(thresholds))
         s64 = r.downloadAov(cam, N.KF_AOV_SUM_F64)
         res["plain"] = plain
         res["plain_check"] = {"frames_in_fp64_sum": float(s64[..., 3].max()), "spp": spp}
@@ -387,13 +398,16 @@ def train_network(path, views=2000, size=256, full_w=1920, full_h=1080, base_spp
             "train_seconds": t_train}
 
 
-def icosphere_eval(networks: dict, width=1920, height=1080, ref_spp=2048, ref_frame_spp=32,
-                   spps=(1, 4, 8, 32, 128), log=print) -> dict:
+def icosphere_eval(networks: dict, width=1920, height=1080, ref_spp=8192, ref_frame_spp=32, plain_frame_spp=8,
+                   plain_checkpoint_step=512, plain_max_spp=16384, spps=(1, 4, 8, 32, 128),
+                   thresholds=(1e-1, 3e-2, 1e-2, 3e-3, 1e-3), log=print) -> dict:
     """The networks (name -> parameter file) on the 256-icosphere scene of seed 0 (glossy,
     metallic and transmissive spheres, 7 lights, RR, depth 8) at width x height: content the
     Cornell-trained networks never saw; a network trained with add_icosphere_views saw
     scenes of other seeds. Reference: two FP64 accumulations of ref_spp / 2 (floor as in
-    run())."""
+    run()). Plain accumulation of 8-spp frames (seed 7) is measured against the same
+    reference until its relMSE reaches the smallest threshold (as in run()), and each
+    network's denoised frames give a time to each threshold."""
     cfg = scenes.icosphere_config(spp=ref_frame_spp, depth=8)
     cfg.setRussianRoulette(True)
     out = {"scene": f"256 icospheres {width}x{height} depth 8", "reference_spp": ref_spp}
@@ -407,13 +421,18 @@ def icosphere_eval(networks: dict, width=1920, height=1080, ref_spp=2048, ref_fr
         log(f"icosphere reference {ref_spp} spp: floor {floor:.3e}")
         del a, b
         timer = _Timer(r)
+        plain, _ = _plain_curve(r, cfg, cam, ref, floor, timer, plain_frame_spp, plain_checkpoint_step,
+                                plain_max_spp, min(thresholds))
+        out["plain"] = plain
+        log("icosphere plain: " + ", ".join(f"{p['spp']}spp {p['relmse']:.3e}" for p in plain))
         flops = unet_flops(height, width)
         for name, path in networks.items():
             d = api.Denoiser(r, seed=0)
             d.load(path)
             log(f"{name} network on the icosphere scene:")
             den = _denoised_frames(r, cfg, cam, d, spps, ref, floor, timer, flops, log)
-            out[name] = [{k: p[k] for k in ("spp", "relmse_noisy", "relmse", "relmse_debiased")} for p in den]
+            out[name] = [{k: p[k] for k in ("spp", "ms", "relmse_noisy", "relmse", "relmse_debiased")} for p in den]
+            out[name + "_time_to_relmse"] = _time_to(plain, den, thresholds)
             d.close()
     return out
 

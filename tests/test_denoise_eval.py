@@ -33,3 +33,49 @@ def test_unet_flops_counts_the_executed_layers():
     assert full == pytest.approx(1088 * 1920 * (per_px - first_32 + first_16))
     # narrow frames (below 96 padded pixels) keep the 32-channel first layer
     assert E.unet_flops(64, 80) == pytest.approx(64 * 80 * per_px)
+
+
+def test_plain_curve_checkpoints_and_stops_at_the_threshold(monkeypatch):
+    """Plain accumulation checkpoints at powers of two up to 1024 spp, then every
+    checkpoint_step spp; it stops at the first checkpoint at or below tau_min, and the
+    time is the sum of the timed frames (evaluations untimed)."""
+
+    class FakeRenderer:
+        frames = 0
+
+        def applyConfig(self):
+            pass
+
+        def run(self):
+            self.frames += 1
+
+        def synchronize(self):
+            pass
+
+        def resetFrame(self):
+            self.frames = 0
+
+    class FakeConfig:
+        def __getattr__(self, name):
+            return lambda *a: None
+
+    class FakeTimer:
+        ms = 2.0
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            pass
+
+    r = FakeRenderer()
+    # relMSE of the running mean falls as 8 / spp
+    monkeypatch.setattr(E, "_fp64_mean", lambda rr, cam: rr.frames * 8)
+    monkeypatch.setattr(E, "_gpu_relmse", lambda rr, spp, ref: 8.0 / spp)
+    plain, spp = E._plain_curve(r, FakeConfig(), None, None, 1e-3, FakeTimer(), 8, 512, 65536, 8.0 / 2560)
+    assert [p["spp"] for p in plain] == [8, 16, 32, 64, 128, 256, 512, 1024, 1536, 2048, 2560]
+    assert spp == 2560 and plain[-1]["ms"] == 2.0 * 2560 / 8
+    assert plain[-1]["relmse_debiased"] == 8.0 / 2560 - 1e-3
+    # never reached: stops at max_spp
+    plain, spp = E._plain_curve(r, FakeConfig(), None, None, 0.0, FakeTimer(), 8, 512, 256, 1e-9)
+    assert spp == 256 and plain[-1]["spp"] == 256
