@@ -283,6 +283,8 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         mat.reserve(nt);
         // traversal stack entries address leaves as 26-bit triangle offsets with a 4-bit count
         KF_REQUIRE(nt < (1ull << 26), KF_ERR_LIMIT, "a scene holds at most 67108863 triangles");
+        // geometry records hold 32-bit vertex offsets
+        KF_REQUIRE(nv < (1ull << 32), KF_ERR_LIMIT, "a scene holds at most 4294967295 vertices");
         KF_REQUIRE(r->cfg.blas_leaf_size >= 1 && r->cfg.blas_leaf_size <= 16, KF_ERR_INVALID_ARGUMENT,
                    "blas_leaf_size must be in [1, 16]");
         // TLAS leaves are stack entries too: 26-bit offsets into the leaf list, <= 16 instances
@@ -487,6 +489,9 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         std::vector<uint4> info;
         std::vector<uchar4> texels;
         for (const HostTexture& t : g_textures) {
+            // texture records hold 32-bit texel offsets
+            KF_REQUIRE(texels.size() + (size_t)t.w * t.h < (1ull << 32), KF_ERR_LIMIT,
+                       "the textures hold at most 4294967295 texels in total");
             info.push_back(make_uint4((uint32_t)texels.size(), t.w, t.h, t.srgb));
             const uchar4* p = reinterpret_cast<const uchar4*>(t.rgba.data());
             texels.insert(texels.end(), p, p + (size_t)t.w * t.h);
