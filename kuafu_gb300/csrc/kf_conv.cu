@@ -709,7 +709,7 @@ bool halo_shape(int Cin, int n_tile, HaloShape& out) {
         if (!((R >= 4 && S == 3) || (R == 2 && S >= 2) || (R == 1 && S == 1))) continue;
         // 32-channel chunks first (64-byte TMA pieces, half the chunk round trips), with three
         // stages or, where those do not fit, two; then 16-channel chunks
-        for (const auto [CK, stages] : {std::pair{32, 3}, std::pair{32, 2}, std::pair{16, 3}, std::pair{16, 2}}) {
+        for (const auto& [CK, stages] : {std::pair{32, 3}, std::pair{32, 2}, std::pair{16, 3}, std::pair{16, 2}}) {
             if (Cin % CK) continue;
             if (R == 8 && stages == 3) continue; // an 8-row halo leaves room for two
             HaloShape h;

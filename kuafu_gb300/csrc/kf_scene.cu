@@ -311,7 +311,6 @@ void scene_sync_gpu(kf_renderer_s* r, kf_scene_s* s) {
         G.geom.upload(geom.data(), geom.size(), st);
 
         // BLAS per geometry, appended to one node pool and one triangle pool.
-        std::vector<Node4> pool_host; // not used: pools are assembled on device
         G.blas_root.assign(ng, 0);
         G.blas_box.assign(ng, {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY});
         G.blas_bound.resize(ng);
