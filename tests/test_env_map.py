@@ -1,6 +1,5 @@
 """Environment cube map (Scene::setEnvironmentMap, scene.cpp:182-188; PathTrace.rmiss:14-29):
 the KTX 1.1 reader, the RGBA8 / sRGB path, and the oracle's cube-face mapping. CPU only."""
-import math
 import struct
 
 import numpy as np
