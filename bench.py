@@ -1,7 +1,7 @@
 """Benchmark: Mrays/s of the GB300 path tracer on the 256-icosphere scene.
 
-Workload (one step = one frame): 256 level-4 icospheres (1.31 M triangles, one
-BLAS each + TLAS), 1 directional + 4 point + 2 spot lights, constant background
+Workload (one step = one frame): 256 level-4 icospheres (1.31 M triangles; the
+identical geometries share one BLAS, + TLAS), 1 directional + 4 point + 2 spot lights, constant background
 0.1, 1920x1080, 8 samples per pixel, path depth 8, Russian roulette from bounce
 4 (kuafu's defaults). Rays = primary + extension + shadow traversals actually
 issued; BVH build is outside the timed region.
@@ -12,8 +12,9 @@ The line also carries "time_to_relmse": the Cornell box at 1920x1080, the learne
 denoiser (trained first on this renderer's own low/high-spp pairs) against plain
 accumulation, both measured until relMSE <= 1e-3 against a 40960-spp FP64
 reference (kuafu_gb300/denoise_eval.py; --no-denoise skips it; N = 1 only). The
-network shipped with the package is evaluated on the same frames, and both networks
-on the icosphere scene (content neither was trained on).
+two networks shipped with the package (Cornell; Cornell and icosphere scenes) are
+evaluated on the same frames, and all three networks on the 1080p icosphere scene
+against plain accumulation there.
 
 Under torchrun (N > 1) every rank renders its own replica of the workload (the
 path has no cross-GPU exchange); value = rays of all ranks / max time over ranks.
@@ -47,6 +48,35 @@ def _dist():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def aggregate_over_ranks(t_ms: float, rays: float, ws: int, device="cpu"):
+    """The job's timed region and work under torchrun: the slowest rank's time (MAX) and
+    the rays of all ranks (SUM), each rank rendering its own replica. One rank: as given."""
+    if ws <= 1:
+        return float(t_ms), float(rays)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(t_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    rr = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(rr, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(rr.item())
+
+
+def _finish_ranks(ws: int):
+    """All ranks leave together: rank 0 prints after its extra passes while the others wait."""
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def mrays_per_s(rays_all: float, t_ms: float) -> float:
+    """Whole-job throughput: all ranks' rays over the slowest rank's time."""
+    return rays_all / (t_ms / 1e3) / 1e6
 
 
 def _peaks():
@@ -526,19 +556,8 @@ def run_ours(args):
     barrier()
     st = r.stats()
     rays = st.rays_primary + st.rays_extension + st.rays_shadow
-    t_ms = sum(times)
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([t_ms], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-        rr = torch.tensor([float(rays)], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(rr)
-        rays_all = float(rr.item())
-    else:
-        rays_all = float(rays)
-    value = rays_all / (t_ms / 1e3) / 1e6
+    t_ms, rays_all = aggregate_over_ranks(sum(times), rays, ws, device=f"cuda:{device}")
+    value = mrays_per_s(rays_all, t_ms)
     rays_per_frame = rays / args.steps
     if args.quick:
         if rank == 0:
@@ -546,6 +565,7 @@ def run_ours(args):
                               "ms_per_step": t_ms / args.steps, "config": dict(WORKLOAD), "clocks": clk,
                               "bvh_build_ms": first_build_ms}), flush=True)
         r.close()
+        _finish_ranks(ws)
         return 0
 
     # e2e: the public API with host buffers: run + download of the BGRA frame per step
@@ -560,7 +580,8 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     st2 = r.stats()
     e2e_rays = st2.rays_primary + st2.rays_extension + st2.rays_shadow
-    e2e_val = e2e_rays / e2e_s / 1e6 * ws
+    e2e_ms, e2e_rays_all = aggregate_over_ranks(e2e_s * 1e3, e2e_rays, ws, device=f"cuda:{device}")
+    e2e_val = mrays_per_s(e2e_rays_all, e2e_ms)
     h2d = C.sizeof(N.kf_camera_ubo) + C.sizeof(N.kf_push_constants) + 32 + C.sizeof(N.kf_dir_light_ubo) + \
         C.sizeof(N.kf_point_lights_ubo) + C.sizeof(N.kf_active_lights_ubo)
 
@@ -669,11 +690,7 @@ def run_ours(args):
         print(json.dumps(result), flush=True)
     else:
         r.close()
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.barrier()
-        dist.destroy_process_group()
+    _finish_ranks(ws)
     return 0
 
 
