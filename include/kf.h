@@ -342,6 +342,10 @@ KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, fl
                            void* stream);
 /* Error word of the tensor-core kernels (0 = none; set when a bounded wait expired); cleared on read. */
 KF_API int kf_tc_error(uint32_t* out);
+/* Self-test of the bounded waits: one kernel waits on an mbarrier that nothing arrives on,
+ * gives up after budget_cycles SM cycles (1 .. 2e9) and sets the error word to 99, which
+ * kf_tc_error then reports; no fault, the context stays usable. */
+KF_API int kf_tc_wait_probe(uint64_t budget_cycles, void* stream);
 
 /* ---- learned denoiser: replaces kuafu's OptiX pass (Config::setUseDenoiser,
  * config.cpp:142; context.cpp:651-670 feeds rgba + albedo + normal to OptiX and

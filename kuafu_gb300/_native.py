@@ -234,6 +234,7 @@ PROTOTYPES = {
     "kf_conv3x3_bf16": (I, [VP, I, I, I, I, VP, I, VP, I, I, VP, I, I, VP]),
     "kf_gemm_bf16_tn": (I, [VP, I, VP, I, I, VP, I, I, VP]),
     "kf_tc_error": (I, [C.POINTER(U32)]),
+    "kf_tc_wait_probe": (I, [C.c_uint64, VP]),
     "kf_denoiser_create": (I, [VP, U32, C.POINTER(VP)]),
     "kf_denoiser_destroy": (I, [VP]),
     "kf_denoiser_num_params": (I, [VP, C.POINTER(C.c_uint64)]),

@@ -1279,6 +1279,12 @@ KF_API int kf_gemm_bf16_tn(const void* a, int m, const void* b, int n, int k, fl
                      splits, static_cast<cudaStream_t>(stream));
     });
 }
+KF_API int kf_tc_wait_probe(uint64_t budget_cycles, void* stream) {
+    return guarded([&] {
+        REQ(budget_cycles <= (uint64_t)INT64_MAX, "budget out of range");
+        tc_wait_probe((long long)budget_cycles, static_cast<cudaStream_t>(stream));
+    });
+}
 KF_API int kf_tc_error(uint32_t* out) {
     return guarded([&] {
         REQ(out, "null argument");

@@ -927,6 +927,26 @@ void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, 
     launch_tc<1, 128, 4>(grid, ma, mb, p, st);
 }
 
+namespace {
+// One thread waits on an mbarrier that nothing arrives on, through the same bounded wait the
+// tensor-core kernels use: it gives up after `budget` SM cycles and records `code`.
+__global__ void k_wait_probe(long long budget, uint32_t code) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_barrier_init();
+        if (!tc::mbar_wait(&bar, 0, budget)) set_error(code);
+    }
+}
+} // namespace
+
+void tc_wait_probe(long long budget_cycles, cudaStream_t st) {
+    KF_REQUIRE(budget_cycles > 0 && budget_cycles <= kWaitBudget, KF_ERR_INVALID_ARGUMENT,
+               "wait probe: budget must be in (0, 2e9] cycles");
+    k_wait_probe<<<1, 32, 0, st>>>(budget_cycles, kWaitProbeError);
+    KF_CUDA_CHECK(cudaGetLastError());
+}
+
 uint32_t tc_take_error() {
     uint32_t e = 0, z = 0;
     KF_CUDA_CHECK(cudaMemcpyFromSymbol(&e, g_tc_error, sizeof(e)));

@@ -32,5 +32,11 @@ void gemm_bf16_tn(const __nv_bfloat16* a, int M, const __nv_bfloat16* b, int N, 
 
 // Reads and clears the error word the tensor-core kernels set when a bounded wait expires.
 uint32_t tc_take_error();
+// Error word a wait probe leaves when its wait gives up.
+constexpr uint32_t kWaitProbeError = 99;
+// Launches a kernel whose wait on a barrier that nothing arrives on gives up after
+// budget_cycles SM cycles and sets the error word to kWaitProbeError (no fault: the
+// context stays usable).
+void tc_wait_probe(long long budget_cycles, cudaStream_t st);
 
 } // namespace kf

@@ -244,6 +244,8 @@ def test_tensor_kernel_arguments_are_checked_before_any_launch():
     assert lib.kf_gemm_bf16_tn(A, 128, A, 64, 64, A, 32, 1, None) == INVALID       # ldd < n
     assert lib.kf_gemm_bf16_tn(A, 128, A, 64, 60, A, 64, 1, None) == INVALID       # k % 8 != 0
     assert lib.kf_gemm_bf16_tn(A + 8, 128, A, 64, 64, A, 64, 1, None) == INVALID   # operand misaligned
+    assert lib.kf_tc_wait_probe(0, None) == INVALID                          # empty budget
+    assert lib.kf_tc_wait_probe(3_000_000_000, None) == INVALID              # beyond the kernels' own
     got = C.c_double()
     assert lib.kf_relmse_noalloc(C.c_void_p(A + 4), C.c_void_p(A), 16, 1e-2, None, C.byref(got)) == INVALID
     assert b"16-byte aligned" in lib.kf_last_error()

@@ -85,3 +85,19 @@ def test_gemm_tn_matches_torch(m, n, k, splits):
     ref = a.float() @ b.float().T
     err = (d - ref).abs().max().item() / (ref.abs().max().item() + 1e-6)
     assert err < 1e-4, f"max error {err:.3e}"
+
+
+def test_bounded_wait_gives_up_reports_and_leaves_the_context_usable():
+    """The tensor-core kernels' bounded wait, made to run out: a kernel waits on an mbarrier
+    that nothing arrives on with a budget of 2e6 SM cycles (about 1 ms). It gives up, and
+    the error word reads 99 once, then 0. The context stays usable: a convolution run after
+    it matches the PyTorch reference."""
+    import torch
+
+    lib = N.load()
+    _tc_error()  # start from a clear error word
+    N.check(lib.kf_tc_wait_probe(2_000_000, torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert _tc_error() == 99
+    assert _tc_error() == 0
+    test_conv3x3_matches_torch(1, 6, 130, 32, 80, 80, True, 80, 0)
