@@ -48,6 +48,7 @@ class Config:
     def getPathDepth(self): return self._c.path_depth
     def getMaxPathDepth(self): return self._c.max_path_depth
     def setRussianRoulette(self, flag): self._c.russian_roulette = int(bool(flag))
+    def getRussianRoulette(self): return bool(self._c.russian_roulette)
     def setRussianRouletteMinBounces(self, n): self._c.rr_min_bounces = int(n)
     def setNextEventEstimation(self, flag): self._c.nee = int(bool(flag))
     def setNextEventEstimationMinBounces(self, n): self._c.nee_min_bounces = int(n)

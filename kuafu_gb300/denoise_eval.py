@@ -157,10 +157,12 @@ def add_icosphere_views(r: api.Kuafu, cfg: api.Config, d: api.Denoiser, count: i
     """Adds `count` training views of icosphere scenes (scenes.icospheres with `spheres`
     level-4 spheres, seed 20000 + v: placements, materials and lights vary) through
     size x size windows of their full_w x full_h 60-degree view, rendered at depth 8 with
-    Russian roulette as the icosphere workload is; each scene is removed once its pairs are
-    stored. Returns the seconds taken."""
+    Russian roulette as the icosphere workload is, then restores cfg's depth and roulette;
+    each scene is removed once its pairs are stored. The renderer's geometry and instance
+    limits must admit `spheres` of each (train_network sets 264). Returns the seconds taken."""
     rng = scenes.SplitMix64(0x1C05F00D)
     t0 = time.perf_counter()
+    depth_before, rr_before = cfg.getPathDepth(), cfg.getRussianRoulette()
     cfg.setPathDepth(8)
     cfg.setRussianRoulette(True)
     try:
@@ -177,8 +179,8 @@ def add_icosphere_views(r: api.Kuafu, cfg: api.Config, d: api.Denoiser, count: i
             if log and (v + 1) % 100 == 0:
                 log(f"icosphere views: {v + 1} of {count} ({time.perf_counter() - t0:.0f} s)")
     finally:
-        cfg.setPathDepth(5)
-        cfg.setRussianRoulette(False)
+        cfg.setPathDepth(depth_before)
+        cfg.setRussianRoulette(rr_before)
         r.applyConfig()
     return time.perf_counter() - t0
 

@@ -23,6 +23,22 @@ def _dirs(cam, px, py):
     return out[:, :3] / np.linalg.norm(out[:, :3], axis=1, keepdims=True)
 
 
+def test_window_camera_at_the_icosphere_views_60_degrees():
+    """The 60-degree icosphere camera (add_icosphere_views) windows the same way."""
+    cfg = scenes.icosphere_config(spp=1, depth=1, count=4)
+    cfg.setHostOnly(True)
+    r = api.Kuafu(cfg)
+    full = scenes.icospheres(r, 1920, 1080, count=4, level=1)
+    s2 = r.createScene()
+    win = scenes.icospheres(r, 256, 256, count=4, level=1, scene=s2)
+    x0, y0 = 700, 90
+    denoise_eval.window_camera(win, 256, 1920, 1080, x0, y0, fov_deg=60.0)
+    rng = np.random.default_rng(4)
+    i = rng.uniform(0, 256, 64)
+    j = rng.uniform(0, 256, 64)
+    assert np.abs(_dirs(win, i, j) - _dirs(full, x0 + i, y0 + j)).max() < 1e-5
+
+
 def test_window_camera_traces_the_rays_of_its_crop():
     cfg = scenes.cornell_config()
     cfg.setHostOnly(True)
