@@ -84,8 +84,9 @@ typedef struct kf_config {
                                       rendering calls then fail with KF_ERR_NO_DEVICE */
     uint32_t traversal;            /* 0: one thread per ray; 1: persistent warps with dynamic
                                       ray fetch (default). Both give identical results. */
-    uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order, fastest build); 1: host binned
-                                      SAH (default: fewer node visits per ray); 2: GPU PLOC
+    uint32_t bvh_builder;          /* 0: GPU LBVH (Morton order); 1: host SAH (default: full
+                                      sweep up to 4096 primitives, binned above, SAH-optimal
+                                      4-wide collapse; fewer node visits per ray); 2: GPU PLOC
                                       (locally-ordered clustering). Same hits. */
     uint32_t dyn_refill_below;     /* persistent traversal: a warp fetches new rays when fewer
                                       lanes than this are busy (1..32, default 16) */

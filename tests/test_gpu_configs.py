@@ -6,7 +6,7 @@
   from bounce 4, 1 directional + 4 point + 2 spot lights, background 0.1 (the Mrays/s
   workload): the GPU renders the whole frame, the oracle traverses its own CPU BVH for
   fixed crops of it (deep BLAS, long traversal stacks, 9-trace paths).
-* All three BVH builders (GPU LBVH, host binned SAH, GPU PLOC) give the same hits and paths.
+* All three BVH builders (GPU LBVH, host SAH, GPU PLOC) give the same hits and paths.
 * Converged FP64 accumulation: the GPU's FP64 sum of 1024 spp against the oracle's FP64
   render, on the same sample streams (agreement far below the noise) and on independent
   streams (agreement within the noise floor of 1024 spp).
@@ -121,7 +121,7 @@ def test_icospheres_full_scene_ray_count(c2_frame):
 @pytest.mark.parametrize("builder", [0, 1, 2])
 @pytest.mark.parametrize("leaf", [1, 4, 16])
 def test_both_bvh_builders_find_the_same_hits(builder, leaf):
-    """GPU LBVH (bvh_builder 0), host binned SAH (1) and GPU PLOC (2) change the tree, never
+    """GPU LBVH (bvh_builder 0), host SAH (1) and GPU PLOC (2) change the tree, never
     the hits."""
     spp, depth = 2, 3
     cfg = scenes.icosphere_config(spp=spp, depth=depth, count=24)
